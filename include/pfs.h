@@ -1,0 +1,192 @@
+/*
+ * pfs.h - C ABI of the GB300 (sm_103a) fluid step library libpfs_gb300.so.
+ *
+ * Drop-in replacement for the per-timestep update of
+ * mdushkoff/Probabilistic_Fluid_Simulation: simulate_fluid_step and
+ * advect_color_step, declared in includes/fluid.hpp:106-119 and implemented
+ * on the CPU in src/fluid.cpp:298-320 (the semantics reproduced here) and on
+ * the GPU in src/fluid.cu:282-317.
+ *
+ * Conventions (kept from the reference):
+ *   - Fields are interleaved HWC float32: velocity (vy, vx, 4) with channels
+ *     u, v, pressure, divergence (src/fluid.cpp:15-17, 234-235, 255); image
+ *     (iy, ix, iz) with any channel count iz.
+ *   - Boundaries are periodic everywhere (src/fluid.cpp:43-57, 159-162).
+ *   - The caller owns every buffer. Calls may swap the caller's pointers, as
+ *     the reference does (src/fluid.cpp:188-194, 260-266, 317-319).
+ *   - Channels 2-3 of both velocity buffers are solver state carried between
+ *     steps: the pressure iteration starts from the previous step's pressure.
+ *
+ * Differences from the reference:
+ *   - Every call returns a status (PFS_OK == 0); the reference returns void
+ *     and never checks a launch. pfs_last_error() describes the last failure
+ *     of the calling thread.
+ *   - NUM_JACOBI_ITERS (includes/fluid.hpp:11, a compile-time 30) is a
+ *     runtime setting, pfs_set_jacobi_iters().
+ *   - Work is issued on the stream set by pfs_set_stream() (default: the
+ *     legacy default stream, as in the reference).
+ *
+ * No torch or CUDA C++ types appear in this interface; streams are passed as
+ * void* (a cudaStream_t).
+ */
+#ifndef PFS_H_
+#define PFS_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ---------------------------------------------------------------- */
+enum {
+    PFS_OK = 0,
+    PFS_ERR_INVALID_ARGUMENT = 1, /* bad dims, null pointers, dt <= 0, ...        */
+    PFS_ERR_CUDA = 2,             /* a CUDA call failed; see pfs_last_error()     */
+    PFS_ERR_NOT_FINITE = 3,       /* NaN/Inf in an input that was checked         */
+    PFS_ERR_UNSUPPORTED = 4,      /* option not available for these sizes         */
+    PFS_ERR_NO_DEVICE = 5,        /* no CUDA device visible                        */
+    PFS_ERR_DEVICE_TIMEOUT = 6    /* a bounded device-side wait ran out            */
+};
+
+/* Human-readable name of a status code. */
+const char *pfs_status_string(int status);
+/* Message of the calling thread's last failed call ("" if none). */
+const char *pfs_last_error(void);
+/* Library version as 10000*major + 100*minor + patch. */
+int pfs_version(void);
+
+/* ---- global settings --------------------------------------------------------- */
+/* Sweep count of both diffusion and pressure per step; replaces
+ * NUM_JACOBI_ITERS (includes/fluid.hpp:11). Default 30. n >= 0. */
+int pfs_set_jacobi_iters(int n);
+int pfs_get_jacobi_iters(void);
+/* Stream for the drop-in calls below (a cudaStream_t, NULL = legacy default). */
+int pfs_set_stream(void *stream);
+/* Free the cached scratch of the drop-in calls on the current device. */
+int pfs_release_workspace(void);
+
+/* ---- drop-in: CUDA branch of includes/fluid.hpp -------------------------------- */
+/*
+ * One timestep on device buffers. Replaces
+ *   void simulate_fluid_step(float **vp, float **tmp, float dt, float viscosity,
+ *                            int vx, int vy, int vz);        (includes/fluid.hpp:107)
+ * with the semantics of src/fluid.cpp:298-310: after the call channels 0-1 of
+ * *vp hold the projected velocity, channel 2 of *tmp the final pressure and
+ * channel 2 of *vp the one before it, channel 3 of both the divergence. vz
+ * must be 4. Asynchronous on the library stream. The scratch (planar copies
+ * of the fields) is allocated on first use per device and grid size and kept
+ * until pfs_release_workspace().
+ */
+int pfs_simulate_fluid_step(float **vp, float **tmp, float dt, float viscosity, int vx, int vy, int vz);
+
+/*
+ * Image advection on device buffers, then swap *image and *itmp. Replaces
+ *   void advect_color_step(float **image, float **itmp, float **vp, float dt,
+ *                          int ix, int iy, int iz, int vx, int vy, int vz);
+ *                                                            (includes/fluid.hpp:116)
+ * with the semantics of src/fluid.cpp:72-127,312-320. Allocates nothing.
+ */
+int pfs_advect_color_step(float **image, float **itmp, float **vp, float dt, int ix, int iy, int iz, int vx, int vy,
+                          int vz);
+
+/* ---- drop-in: CPU branch of includes/fluid.hpp (host buffers, GPU compute) ----- */
+/* Same layout as vp_field (includes/fluid.hpp:17-22). */
+typedef struct {
+    int x;
+    int y;
+    int z;
+    float *data;
+} pfs_vp_field;
+
+/*
+ * Replaces void simulate_fluid_step(vp_field *vp, vp_field *tmp, float dt,
+ * float viscosity) (includes/fluid.hpp:109): host buffers in, host buffers
+ * out, computed on the GPU (copies in, step, copies out; returns when the
+ * host buffers hold the result). Pinned host memory copies fastest.
+ */
+int pfs_simulate_fluid_step_host(pfs_vp_field *vp, pfs_vp_field *tmp, float dt, float viscosity);
+/* Replaces void advect_color_step(vp_field *image, vp_field *itmp, vp_field *vp,
+ * float dt) (includes/fluid.hpp:118); swaps image->data and itmp->data. */
+int pfs_advect_color_step_host(pfs_vp_field *image, pfs_vp_field *itmp, pfs_vp_field *vp, float dt);
+
+/* ---- sessions: state kept on the device across steps ----------------------------- */
+/*
+ * A session holds one simulation resident in HBM in planar layout (one plane
+ * per channel) and advances it many steps per call. It generalises the
+ * reference loop (src/main.cpp:219-246: simulate_fluid_step then
+ * advect_color_step) with:
+ *   - separate diffusion and pressure sweep counts,
+ *   - an optional residual stop: the pressure iteration ends at the first
+ *     check point (every check_every sweeps, and at max_iters) where
+ *     ||b - A p||_2 / ||b||_2 <= tol, A the 5-point periodic operator of
+ *     src/fluid.cpp:239-257, evaluated per cell in FP64,
+ *   - the buffer roles of src/fluid.cpp kept exactly (which buffer's
+ *     pressure seeds the next solve depends on the sweep-count parities).
+ * With tol <= 0 and diffuse_iters == max_iters == N, a step equals the
+ * reference built with NUM_JACOBI_ITERS = N.
+ */
+enum { PFS_HOST = 0, PFS_DEVICE = 1 };
+
+typedef struct {
+    float dt;
+    float viscosity;
+    int diffuse_iters;  /* diffusion sweeps per step (reference: NUM_JACOBI_ITERS) */
+    int max_iters;      /* pressure sweeps (fixed mode) or cap (residual mode)      */
+    double tol;         /* > 0: residual mode; <= 0: exactly max_iters sweeps       */
+    int check_every;    /* residual check interval in sweeps (0: only at the cap)   */
+    int fuse_depth;     /* sweeps fused per launch, 0 = tuned default              */
+    int chunk_rows;     /* rows per warp in the fused sweep, 0 = tuned default      */
+    int want_residual;  /* fixed mode: also report the final residual              */
+} pfs_params;
+
+typedef struct {
+    int sweeps;          /* pressure sweeps of the last step               */
+    int checks;          /* residual evaluations of the last step          */
+    double rel_residual; /* last evaluated relative residual (-1 if none)   */
+    double bnorm;        /* ||b||_2 of the last step                        */
+    int capped;          /* last step stopped at max_iters above tol        */
+    long long steps;     /* steps run by this session                       */
+    long long total_sweeps;
+    long long cap_hits;
+} pfs_stats;
+
+typedef struct pfs_session pfs_session;
+
+/* Defaults: dt 0.1, viscosity 0, 30/30 sweeps, fixed mode. */
+void pfs_params_default(pfs_params *p);
+/* vx, vy: velocity grid; ix, iy, iz: image (iz = 0 for no image). */
+int pfs_session_create(pfs_session **out, int vx, int vy, int ix, int iy, int iz, const pfs_params *params,
+                       void *stream);
+int pfs_session_set_params(pfs_session *s, const pfs_params *params);
+/* Load state from interleaved buffers (vp, tmp: (vy, vx, 4); image (iy, ix, iz)),
+ * host or device pointers per `where`. image may be NULL when iz == 0. */
+int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const float *image, int where);
+/* Advance n steps (asynchronous unless the residual mode needs a host decision). */
+int pfs_session_step(pfs_session *s, int n);
+/* Write the state back in the reference layout (the buffers the reference's
+ * vp, tmp and image pointers would designate after the same steps). */
+int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, int where);
+int pfs_session_stats(pfs_session *s, pfs_stats *out);
+int pfs_session_sync(pfs_session *s);
+int pfs_session_destroy(pfs_session *s);
+
+/* ---- kernel-level entry points (tests, tuning, benchmarks) ------------------------ */
+/*
+ * `levels` pressure Jacobi sweeps (src/fluid.cpp:239-257) on planar fields:
+ * p_out = J^levels(p_in) with divergence plane b; planes have row pitch ld
+ * floats. fused != 0 uses the temporally blocked kernel (requires vx % 4 == 0,
+ * ld % 4 == 0, 16-byte aligned planes); p_prev, if non-NULL, receives
+ * J^(levels-1)(p_in). No allocation.
+ */
+int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *p_prev, int vx, int vy, int ld,
+                        int levels, int fused, int chunk_rows, void *stream);
+/* ||b - A p||_2^2 and ||b||_2^2 (FP64) of planar p, b; blocking. */
+int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, double *rr, double *bb,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFS_H_ */

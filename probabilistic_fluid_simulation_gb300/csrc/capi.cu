@@ -1,0 +1,783 @@
+// C ABI of libpfs_gb300.so (include/pfs.h): drop-in step calls, sessions and
+// kernel-level entry points, plus the host orchestration of one timestep.
+//
+// Buffer roles. The reference ping-pongs two interleaved buffers and swaps
+// the caller's pointers (src/fluid.cpp:188-194, 260-266); which buffer ends
+// up holding which iterate depends on the sweep counts. Here the fields live
+// in planar form: two velocity slots (u, v planes) standing for the
+// reference's two buffers, three pressure planes, and one divergence plane.
+// The orchestration below tracks, exactly as the reference's pointer swaps
+// would, which slot plays "vp" and "tmp" after each phase and which pressure
+// plane is each slot's channel 2, so every channel of both buffers can be
+// written back as the reference leaves it.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <utility>
+
+#include "kernels.h"
+#include "pfs.h"
+
+using pfs::Reduce;
+
+namespace {
+
+thread_local std::string g_err;
+std::mutex g_mu;
+int g_iters = 30;
+cudaStream_t g_stream = nullptr;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(x)                                                                                              \
+    do {                                                                                                   \
+        cudaError_t e_ = (x);                                                                              \
+        if (e_ != cudaSuccess)                                                                             \
+            return fail(PFS_ERR_CUDA, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define CKS(x)                      \
+    do {                            \
+        int s_ = (x);               \
+        if (s_ != PFS_OK) return s_; \
+    } while (0)
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// ---------------------------------------------------------------------------------------------
+// Planar fields of one velocity grid.
+struct Field {
+    int dev = -1, w = 0, h = 0, ld = 0;
+    size_t plane = 0;  // floats per plane
+    float *mem = nullptr;
+    float *u[2] = {nullptr, nullptr}, *v[2] = {nullptr, nullptr}, *p[3] = {nullptr, nullptr, nullptr};
+    float *b = nullptr;
+    int pidx[2] = {0, 1};  // pressure plane holding channel 2 of velocity slot 0 / 1
+    double *rmem = nullptr;
+    unsigned *ticket = nullptr;
+    double *hres = nullptr;  // pinned, [2]
+    Reduce red{};
+
+    int alloc(int w_, int h_)
+    {
+        release();
+        CK(cudaGetDevice(&dev));
+        w = w_;
+        h = h_;
+        ld = round_up(w, 32);
+        plane = (size_t)ld * h;
+        CK(cudaMalloc(&mem, plane * 8 * sizeof(float)));
+        CK(cudaMemset(mem, 0, plane * 8 * sizeof(float)));
+        u[0] = mem;
+        u[1] = mem + plane;
+        v[0] = mem + 2 * plane;
+        v[1] = mem + 3 * plane;
+        p[0] = mem + 4 * plane;
+        p[1] = mem + 5 * plane;
+        p[2] = mem + 6 * plane;
+        b = mem + 7 * plane;
+        pidx[0] = 0;
+        pidx[1] = 1;
+        const int nb = pfs::kReduceBlocks;
+        CK(cudaMalloc(&rmem, (2 * nb + 2) * sizeof(double) + 16));
+        CK(cudaMemset(rmem, 0, (2 * nb + 2) * sizeof(double) + 16));
+        ticket = reinterpret_cast<unsigned *>(rmem + 2 * nb + 2);
+        CK(cudaMallocHost(&hres, 2 * sizeof(double)));
+        red.partials = rmem;
+        red.result = rmem + 2 * nb;
+        red.ticket = ticket;
+        red.nblocks = nb;
+        return PFS_OK;
+    }
+    void release()
+    {
+        if (mem) cudaFree(mem);
+        if (rmem) cudaFree(rmem);
+        if (hres) cudaFreeHost(hres);
+        mem = nullptr;
+        rmem = nullptr;
+        hres = nullptr;
+        w = h = 0;
+    }
+    ~Field() { release(); }
+};
+
+struct Tuning {
+    int levels = 8;  // sweeps fused per launch
+    int halo = 8;    // halo columns per side of a warp strip (>= levels)
+    int chunk = 32;  // rows per warp
+};
+
+struct StepCfg {
+    float dt = 0.1f, visc = 0.0f;
+    int D = 30, S = 30;
+    double tol = 0.0;
+    int check_every = 0;
+    bool want_res = false;
+    Tuning tun;
+};
+
+struct StepOut {
+    int sweeps = 0, checks = 0;
+    double rel = -1.0, bnorm = -1.0;
+    bool capped = false;
+};
+
+bool fused_ok(const Field &f) { return f.w % 4 == 0; }
+
+// Sum r^2 of pressure plane `pp` and read back (r^2, b^2) (b^2 from the last divergence).
+int residual_host(Field &f, const float *pp, cudaStream_t st, double &rr, double &bb)
+{
+    CK(pfs::launch_residual(pp, f.b, f.ld, f.w, f.h, f.red, st));
+    CK(cudaMemcpyAsync(f.hres, f.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    rr = f.hres[0];
+    bb = f.hres[1];
+    return PFS_OK;
+}
+
+double relative(double rr, double bb) { return bb > 0.0 ? std::sqrt(rr) / std::sqrt(bb) : std::sqrt(rr); }
+
+// Pressure iteration of src/fluid.cpp:239-266 from slot X's plane (q_0) with
+// Y's plane as the other buffer. Afterwards `cur` holds q_S and `prev` q_{S-1}.
+int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStream_t st, int &cur, int &prev)
+{
+    cur = f.pidx[X];
+    prev = f.pidx[Y];
+    int freep = 3 - cur - prev;
+    const bool fused = fused_ok(f);
+    const int L = std::max(1, std::min(c.tun.levels, c.tun.halo));
+    int S = 0;
+    while (S < c.S) {
+        int stop = c.S;
+        if (c.tol > 0.0 && c.check_every > 0) stop = std::min(c.S, (S / c.check_every + 1) * c.check_every);
+        while (S < stop) {
+            if (!fused) {
+                CK(pfs::launch_sweep_single(f.p[cur], f.b, f.p[freep], f.ld, f.w, f.h, st));
+                const int old_prev = prev;
+                prev = cur;
+                cur = freep;
+                freep = old_prev;
+                S += 1;
+                continue;
+            }
+            const int n = std::min(L, stop - S);
+            const bool last = (S + n == stop);
+            CK(pfs::launch_sweep_stream(f.p[cur], f.b, f.p[freep], last ? f.p[prev] : nullptr, f.ld, f.w, f.h, n,
+                                        c.tun.halo, c.tun.chunk, st));
+            if (last) {
+                const int old_cur = cur;
+                cur = freep;  // q_S
+                freep = old_cur;
+                // prev now holds q_{S-1}
+            } else {
+                const int old_cur = cur;
+                cur = freep;
+                freep = old_cur;
+            }
+            S += n;
+        }
+        if (c.tol > 0.0) {
+            double rr, bb;
+            CKS(residual_host(f, f.p[cur], st, rr, bb));
+            o.checks++;
+            o.bnorm = std::sqrt(bb);
+            o.rel = relative(rr, bb);
+            if (o.rel <= c.tol) break;
+        }
+    }
+    o.sweeps = S;
+    o.capped = c.tol > 0.0 && S == c.S && !(o.rel <= c.tol);
+    if (c.want_res && !(c.tol > 0.0)) {
+        double rr, bb;
+        CKS(residual_host(f, f.p[cur], st, rr, bb));
+        o.bnorm = std::sqrt(bb);
+        o.rel = relative(rr, bb);
+    }
+    return PFS_OK;
+}
+
+// Advection, diffusion, divergence and pressure of one step
+// (src/fluid.cpp:298-304). `vp`/`tmp` are the velocity slots playing the
+// reference's vp/tmp on entry. On return Z (the buffer projection reads, the
+// reference's tmp after computePressure) and W (the one it writes, the
+// reference's vp) are set; the caller projects Z -> W.
+int velocity_phase(Field &f, int vp, int tmp, const StepCfg &c, StepOut &o, cudaStream_t st, int &Z, int &W)
+{
+    const int A = vp, B = tmp;
+    // advect(vp, tmp): src/fluid.cpp:300
+    CK(pfs::launch_advect(f.u[A], f.v[A], f.u[B], f.v[B], f.ld, f.w, f.h, c.dt, st));
+
+    // diffuse(tmp, vp): src/fluid.cpp:301. X ends as the reference's vp (it holds
+    // the last diffusion iterate), Y as its tmp.
+    int X = A, Y = B;
+    if (c.D > 0) {
+        if (c.visc == 0.0f) {
+            // alpha = 0, beta = 1: every sweep returns its input (up to the sign
+            // of zero), so all iterates equal the advected field; both slots get it.
+            CK(cudaMemcpyAsync(f.u[A], f.u[B], f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(f.v[A], f.v[B], f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            X = (c.D % 2) ? A : B;
+            Y = (X == A) ? B : A;
+        } else {
+            const float alpha = c.visc * c.dt;
+            const float beta = (float)(1.0 + 4.0 * (double)alpha);
+            int src = B, dst = A;
+            for (int k = 0; k < c.D; ++k) {
+                CK(pfs::launch_diffuse_sweep(f.u[src], f.v[src], f.u[dst], f.v[dst], f.ld, f.w, f.h, alpha, beta, st));
+                if (k != c.D - 1) std::swap(src, dst);
+            }
+            X = dst;
+            Y = src;
+        }
+    }
+
+    // computePressure(vp, tmp): src/fluid.cpp:303
+    const float gamma = (float)(-1.0 / (double)c.dt);
+    CK(pfs::launch_divergence(f.u[X], f.v[X], f.b, f.ld, f.w, f.h, gamma, f.red, st));
+    int cur = f.pidx[X], prev = f.pidx[Y];
+    CKS(pressure_solve(f, X, Y, c, o, st, cur, prev));
+    const int S = o.sweeps;
+    if (S == 0) {
+        Z = Y;
+        W = X;
+    } else {
+        Z = (S % 2) ? Y : X;  // the reference's tmp after S-1 swaps
+        W = (Z == X) ? Y : X;
+        f.pidx[Z] = cur;
+        f.pidx[W] = prev;
+    }
+    return PFS_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Drop-in scratch: one Field per (device, grid), plus interleaved staging for host buffers.
+struct Workspace {
+    Field f;
+    float *stage = nullptr;  // host-call staging: 2 velocity buffers
+    size_t stage_bytes = 0;
+    ~Workspace()
+    {
+        if (stage) cudaFree(stage);
+    }
+};
+std::map<int, Workspace *> g_ws;  // keyed by device
+
+int get_workspace(int w, int h, Workspace **out)
+{
+    int dev;
+    CK(cudaGetDevice(&dev));
+    Workspace *&ws = g_ws[dev];
+    if (!ws) ws = new (std::nothrow) Workspace();
+    if (!ws) return fail(PFS_ERR_CUDA, "out of host memory");
+    if (ws->f.w != w || ws->f.h != h) CKS(ws->f.alloc(w, h));
+    *out = ws;
+    return PFS_OK;
+}
+
+int check_dims(int vx, int vy, int vz, float dt)
+{
+    if (vx <= 0 || vy <= 0) return fail(PFS_ERR_INVALID_ARGUMENT, "grid %dx%d must be positive", vx, vy);
+    if ((long long)vx * vy > (1LL << 30)) return fail(PFS_ERR_INVALID_ARGUMENT, "grid %dx%d too large", vx, vy);
+    if (vz != 4) return fail(PFS_ERR_INVALID_ARGUMENT, "velocity fields have 4 channels, got vz=%d", vz);
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(PFS_ERR_INVALID_ARGUMENT, "dt must be finite and > 0");
+    return PFS_OK;
+}
+
+StepCfg dropin_cfg(float dt, float visc)
+{
+    StepCfg c;
+    c.dt = dt;
+    c.visc = visc;
+    c.D = g_iters;
+    c.S = g_iters;
+    return c;
+}
+
+// Device-pointer step on interleaved buffers A (vp) and B (tmp).
+int dropin_step(float *A, float *B, int w, int h, float dt, float visc, cudaStream_t st)
+{
+    Workspace *ws;
+    CKS(get_workspace(w, h, &ws));
+    Field &f = ws->f;
+    f.pidx[0] = 0;
+    f.pidx[1] = 1;
+    CK(pfs::launch_split_velocity(A, f.u[0], f.v[0], f.ld, w, h, st));
+    CK(pfs::launch_split_channel(A, 2, 4, f.p[0], f.ld, w, h, st));
+    CK(pfs::launch_split_channel(B, 2, 4, f.p[1], f.ld, w, h, st));
+    StepCfg c = dropin_cfg(dt, visc);
+    StepOut o;
+    int Z, W;
+    CKS(velocity_phase(f, 0, 1, c, o, st, Z, W));
+    // subtractPressureGradient(tmp, vp): src/fluid.cpp:304
+    CK(pfs::launch_project(f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.u[W], f.v[W], f.ld, w, h, dt, st));
+    // With equal diffusion and pressure counts the roles always come back as
+    // W = vp, Z = tmp, so the caller's pointers keep their buffers.
+    CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, w, h, st));
+    CK(pfs::launch_merge_velocity(B, f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.b, f.ld, w, h, st));
+    return PFS_OK;
+}
+
+}  // namespace
+
+// =============================================================================================
+// Public C ABI
+// =============================================================================================
+
+struct pfs_session {
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    Field f;
+    int vpSlot = 0, tmpSlot = 1;
+    int iw = 0, ih = 0, ic = 0, ild = 0;
+    size_t iplane = 0;
+    float *img_mem = nullptr;
+    float *img[2] = {nullptr, nullptr};
+    int icur = 0;
+    float *stage = nullptr;
+    size_t stage_bytes = 0;
+    pfs_params prm{};
+    pfs_stats stats{};
+    ~pfs_session()
+    {
+        if (img_mem) cudaFree(img_mem);
+        if (stage) cudaFree(stage);
+    }
+};
+
+extern "C" {
+
+const char *pfs_status_string(int s)
+{
+    switch (s) {
+    case PFS_OK: return "ok";
+    case PFS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case PFS_ERR_CUDA: return "CUDA error";
+    case PFS_ERR_NOT_FINITE: return "non-finite input";
+    case PFS_ERR_UNSUPPORTED: return "unsupported";
+    case PFS_ERR_NO_DEVICE: return "no CUDA device";
+    case PFS_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+const char *pfs_last_error(void) { return g_err.c_str(); }
+
+int pfs_version(void) { return 100; }
+
+int pfs_set_jacobi_iters(int n)
+{
+    if (n < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "sweep count must be >= 0");
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_iters = n;
+    return PFS_OK;
+}
+
+int pfs_get_jacobi_iters(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_iters;
+}
+
+int pfs_set_stream(void *stream)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_stream = (cudaStream_t)stream;
+    return PFS_OK;
+}
+
+int pfs_release_workspace(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    int dev;
+    CK(cudaGetDevice(&dev));
+    auto it = g_ws.find(dev);
+    if (it != g_ws.end()) {
+        CK(cudaDeviceSynchronize());
+        delete it->second;
+        g_ws.erase(it);
+    }
+    return PFS_OK;
+}
+
+int pfs_simulate_fluid_step(float **vp, float **tmp, float dt, float viscosity, int vx, int vy, int vz)
+{
+    if (!vp || !tmp || !*vp || !*tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "null buffer");
+    if (*vp == *tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "vp and tmp must be distinct buffers");
+    CKS(check_dims(vx, vy, vz, dt));
+    if (!std::isfinite(viscosity)) return fail(PFS_ERR_NOT_FINITE, "viscosity must be finite");
+    std::lock_guard<std::mutex> lk(g_mu);
+    return dropin_step(*vp, *tmp, vx, vy, dt, viscosity, g_stream);
+}
+
+int pfs_advect_color_step(float **image, float **itmp, float **vp, float dt, int ix, int iy, int iz, int vx, int vy,
+                          int vz)
+{
+    if (!image || !itmp || !vp || !*image || !*itmp || !*vp) return fail(PFS_ERR_INVALID_ARGUMENT, "null buffer");
+    if (*image == *itmp) return fail(PFS_ERR_INVALID_ARGUMENT, "image and itmp must be distinct buffers");
+    if (ix <= 0 || iy <= 0 || iz <= 0) return fail(PFS_ERR_INVALID_ARGUMENT, "bad image dims");
+    CKS(check_dims(vx, vy, vz, dt));
+    cudaStream_t st;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        st = g_stream;
+    }
+    CK(pfs::launch_advect_image_interleaved(*image, *itmp, ix, iy, iz, *vp, vx, vy, dt, st));
+    std::swap(*image, *itmp);  // src/fluid.cpp:317-319
+    return PFS_OK;
+}
+
+int pfs_simulate_fluid_step_host(pfs_vp_field *vp, pfs_vp_field *tmp, float dt, float viscosity)
+{
+    if (!vp || !tmp || !vp->data || !tmp->data) return fail(PFS_ERR_INVALID_ARGUMENT, "null buffer");
+    if (vp->x != tmp->x || vp->y != tmp->y || vp->z != tmp->z)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "vp and tmp dims differ");
+    CKS(check_dims(vp->x, vp->y, vp->z, dt));
+    if (!std::isfinite(viscosity)) return fail(PFS_ERR_NOT_FINITE, "viscosity must be finite");
+    std::lock_guard<std::mutex> lk(g_mu);
+    const int w = vp->x, h = vp->y;
+    Workspace *ws;
+    CKS(get_workspace(w, h, &ws));
+    const size_t bytes = (size_t)w * h * 4 * sizeof(float);
+    if (ws->stage_bytes < 2 * bytes) {
+        if (ws->stage) cudaFree(ws->stage);
+        ws->stage = nullptr;
+        ws->stage_bytes = 0;
+        CK(cudaMalloc(&ws->stage, 2 * bytes));
+        ws->stage_bytes = 2 * bytes;
+    }
+    float *A = ws->stage, *B = ws->stage + (size_t)w * h * 4;
+    cudaStream_t st = g_stream;
+    CK(cudaMemcpyAsync(A, vp->data, bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B, tmp->data, bytes, cudaMemcpyHostToDevice, st));
+    CKS(dropin_step(A, B, w, h, dt, viscosity, st));
+    CK(cudaMemcpyAsync(vp->data, A, bytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(tmp->data, B, bytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return PFS_OK;
+}
+
+int pfs_advect_color_step_host(pfs_vp_field *image, pfs_vp_field *itmp, pfs_vp_field *vp, float dt)
+{
+    if (!image || !itmp || !vp || !image->data || !itmp->data || !vp->data)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "null buffer");
+    if (image->x <= 0 || image->y <= 0 || image->z <= 0) return fail(PFS_ERR_INVALID_ARGUMENT, "bad image dims");
+    if (itmp->x != image->x || itmp->y != image->y || itmp->z != image->z)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "image and itmp dims differ");
+    CKS(check_dims(vp->x, vp->y, vp->z, dt));
+    std::lock_guard<std::mutex> lk(g_mu);
+    Workspace *ws;
+    CKS(get_workspace(vp->x, vp->y, &ws));
+    const size_t vbytes = (size_t)vp->x * vp->y * 4 * sizeof(float);
+    const size_t ibytes = (size_t)image->x * image->y * image->z * sizeof(float);
+    const size_t need = vbytes + 2 * ibytes;
+    if (ws->stage_bytes < need) {
+        if (ws->stage) cudaFree(ws->stage);
+        ws->stage = nullptr;
+        ws->stage_bytes = 0;
+        CK(cudaMalloc(&ws->stage, need));
+        ws->stage_bytes = need;
+    }
+    float *V = ws->stage, *I = ws->stage + vbytes / sizeof(float), *T = I + ibytes / sizeof(float);
+    cudaStream_t st = g_stream;
+    CK(cudaMemcpyAsync(V, vp->data, vbytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(I, image->data, ibytes, cudaMemcpyHostToDevice, st));
+    CK(pfs::launch_advect_image_interleaved(I, T, image->x, image->y, image->z, V, vp->x, vp->y, dt, st));
+    CK(cudaMemcpyAsync(itmp->data, T, ibytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    std::swap(image->data, itmp->data);  // src/fluid.cpp:317-319
+    return PFS_OK;
+}
+
+// ---- sessions ------------------------------------------------------------------------------
+
+void pfs_params_default(pfs_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->dt = 0.1f;
+    p->viscosity = 0.0f;
+    p->diffuse_iters = 30;
+    p->max_iters = 30;
+    p->tol = 0.0;
+    p->check_every = 0;
+    p->fuse_depth = 0;
+    p->chunk_rows = 0;
+    p->want_residual = 0;
+}
+
+static int check_params(const pfs_params *p)
+{
+    if (!p) return fail(PFS_ERR_INVALID_ARGUMENT, "null params");
+    if (!(p->dt > 0.0f) || !std::isfinite(p->dt)) return fail(PFS_ERR_INVALID_ARGUMENT, "dt must be finite and > 0");
+    if (!std::isfinite(p->viscosity)) return fail(PFS_ERR_NOT_FINITE, "viscosity must be finite");
+    if (p->diffuse_iters < 0 || p->max_iters < 0 || p->check_every < 0)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "sweep counts must be >= 0");
+    if (p->fuse_depth < 0 || p->fuse_depth > 8) return fail(PFS_ERR_INVALID_ARGUMENT, "fuse_depth in [0, 8]");
+    if (p->chunk_rows < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "chunk_rows must be >= 0");
+    if (std::isnan(p->tol)) return fail(PFS_ERR_NOT_FINITE, "tol is NaN");
+    return PFS_OK;
+}
+
+static StepCfg session_cfg(const pfs_session *s)
+{
+    StepCfg c;
+    c.dt = s->prm.dt;
+    c.visc = s->prm.viscosity;
+    c.D = s->prm.diffuse_iters;
+    c.S = s->prm.max_iters;
+    c.tol = s->prm.tol;
+    c.check_every = s->prm.check_every;
+    c.want_res = s->prm.want_residual != 0;
+    if (s->prm.fuse_depth > 0) c.tun.levels = s->prm.fuse_depth;
+    c.tun.halo = c.tun.levels <= 4 ? 4 : 8;
+    if (s->prm.chunk_rows > 0) c.tun.chunk = s->prm.chunk_rows;
+    return c;
+}
+
+int pfs_session_create(pfs_session **out, int vx, int vy, int ix, int iy, int iz, const pfs_params *params,
+                       void *stream)
+{
+    if (!out) return fail(PFS_ERR_INVALID_ARGUMENT, "null output");
+    *out = nullptr;
+    pfs_params def;
+    pfs_params_default(&def);
+    const pfs_params *p = params ? params : &def;
+    CKS(check_params(p));
+    CKS(check_dims(vx, vy, 4, p->dt));
+    if (iz < 0 || (iz > 0 && (ix <= 0 || iy <= 0))) return fail(PFS_ERR_INVALID_ARGUMENT, "bad image dims");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PFS_ERR_NO_DEVICE, "no CUDA device");
+    pfs_session *s = new (std::nothrow) pfs_session();
+    if (!s) return fail(PFS_ERR_CUDA, "out of host memory");
+    s->prm = *p;
+    s->st = (cudaStream_t)stream;
+    int rc = s->f.alloc(vx, vy);
+    if (rc == PFS_OK) CK(cudaGetDevice(&s->dev));
+    if (rc == PFS_OK && iz > 0) {
+        s->iw = ix;
+        s->ih = iy;
+        s->ic = iz;
+        s->ild = round_up(ix, 32);
+        s->iplane = (size_t)s->ild * iy;
+        cudaError_t e = cudaMalloc(&s->img_mem, 2 * s->iplane * iz * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(s->img_mem, 0, 2 * s->iplane * iz * sizeof(float));
+        if (e != cudaSuccess) rc = fail(PFS_ERR_CUDA, "image allocation: %s", cudaGetErrorString(e));
+        s->img[0] = s->img_mem;
+        s->img[1] = s->img_mem + s->iplane * iz;
+    }
+    if (rc != PFS_OK) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return PFS_OK;
+}
+
+int pfs_session_set_params(pfs_session *s, const pfs_params *params)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    CKS(check_params(params));
+    s->prm = *params;
+    return PFS_OK;
+}
+
+static int session_stage(pfs_session *s, size_t bytes)
+{
+    if (s->stage_bytes >= bytes) return PFS_OK;
+    if (s->stage) cudaFree(s->stage);
+    s->stage = nullptr;
+    s->stage_bytes = 0;
+    CK(cudaMalloc(&s->stage, bytes));
+    s->stage_bytes = bytes;
+    return PFS_OK;
+}
+
+int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const float *image, int where)
+{
+    if (!s || !vp || !tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
+    if (s->ic > 0 && !image) return fail(PFS_ERR_INVALID_ARGUMENT, "session has an image: pass it");
+    Field &f = s->f;
+    const size_t vcount = (size_t)f.w * f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
+    const float *A = vp, *B = tmp, *I = image;
+    if (where == PFS_HOST) {
+        CKS(session_stage(s, (2 * vcount + icount) * sizeof(float)));
+        float *dA = s->stage, *dB = s->stage + vcount, *dI = s->stage + 2 * vcount;
+        CK(cudaMemcpyAsync(dA, vp, vcount * sizeof(float), cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(dB, tmp, vcount * sizeof(float), cudaMemcpyHostToDevice, s->st));
+        if (icount) CK(cudaMemcpyAsync(dI, image, icount * sizeof(float), cudaMemcpyHostToDevice, s->st));
+        A = dA;
+        B = dB;
+        I = dI;
+    } else if (where != PFS_DEVICE) {
+        return fail(PFS_ERR_INVALID_ARGUMENT, "where must be PFS_HOST or PFS_DEVICE");
+    }
+    f.pidx[0] = 0;
+    f.pidx[1] = 1;
+    s->vpSlot = 0;
+    s->tmpSlot = 1;
+    CK(pfs::launch_split_velocity(A, f.u[0], f.v[0], f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_velocity(B, f.u[1], f.v[1], f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_channel(A, 2, 4, f.p[0], f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_channel(B, 2, 4, f.p[1], f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_channel(A, 3, 4, f.b, f.ld, f.w, f.h, s->st));
+    if (s->ic > 0) {
+        s->icur = 0;
+        CK(pfs::launch_split_image(I, s->img[0], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
+    }
+    if (where == PFS_HOST) CK(cudaStreamSynchronize(s->st));
+    return PFS_OK;
+}
+
+int pfs_session_step(pfs_session *s, int n)
+{
+    if (!s || n < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "bad session or step count");
+    Field &f = s->f;
+    const StepCfg c = session_cfg(s);
+    for (int k = 0; k < n; ++k) {
+        StepOut o;
+        int Z, W;
+        CKS(velocity_phase(f, s->vpSlot, s->tmpSlot, c, o, s->st, Z, W));
+        const float *pz = f.p[f.pidx[Z]];
+        if (s->ic > 0 && s->iw == f.w && s->ih == f.h) {
+            float *src = s->img[s->icur], *dst = s->img[1 - s->icur];
+            CK(pfs::launch_project_advect_image(f.u[Z], f.v[Z], pz, f.u[W], f.v[W], f.ld, f.w, f.h, c.dt, src, dst,
+                                                s->iplane, s->ic, s->st));
+            s->icur = 1 - s->icur;
+        } else {
+            CK(pfs::launch_project(f.u[Z], f.v[Z], pz, f.u[W], f.v[W], f.ld, f.w, f.h, c.dt, s->st));
+            if (s->ic > 0) {
+                float *src = s->img[s->icur], *dst = s->img[1 - s->icur];
+                CK(pfs::launch_advect_image_planar(src, dst, s->iplane, s->ild, s->iw, s->ih, s->ic, f.u[W], f.v[W],
+                                                   f.ld, f.w, f.h, c.dt, s->st));
+                s->icur = 1 - s->icur;
+            }
+        }
+        s->vpSlot = W;
+        s->tmpSlot = Z;
+        s->stats.sweeps = o.sweeps;
+        s->stats.checks = o.checks;
+        s->stats.rel_residual = o.rel;
+        s->stats.bnorm = o.bnorm;
+        s->stats.capped = o.capped ? 1 : 0;
+        s->stats.steps += 1;
+        s->stats.total_sweeps += o.sweeps;
+        s->stats.cap_hits += o.capped ? 1 : 0;
+    }
+    return PFS_OK;
+}
+
+int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, int where)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    Field &f = s->f;
+    const size_t vcount = (size_t)f.w * f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
+    float *A = vp, *B = tmp, *I = image;
+    if (where == PFS_HOST) {
+        CKS(session_stage(s, (2 * vcount + icount) * sizeof(float)));
+        A = vp ? s->stage : nullptr;
+        B = tmp ? s->stage + vcount : nullptr;
+        I = (image && icount) ? s->stage + 2 * vcount : nullptr;
+    } else if (where != PFS_DEVICE) {
+        return fail(PFS_ERR_INVALID_ARGUMENT, "where must be PFS_HOST or PFS_DEVICE");
+    }
+    const int W = s->vpSlot, Z = s->tmpSlot;
+    if (A) CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, f.w, f.h, s->st));
+    if (B) CK(pfs::launch_merge_velocity(B, f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.b, f.ld, f.w, f.h, s->st));
+    if (I && s->ic > 0)
+        CK(pfs::launch_merge_image(I, s->img[s->icur], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
+    if (where == PFS_HOST) {
+        if (vp) CK(cudaMemcpyAsync(vp, A, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        if (tmp) CK(cudaMemcpyAsync(tmp, B, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        if (I) CK(cudaMemcpyAsync(image, I, icount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+    }
+    return PFS_OK;
+}
+
+int pfs_session_stats(pfs_session *s, pfs_stats *out)
+{
+    if (!s || !out) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
+    *out = s->stats;
+    return PFS_OK;
+}
+
+int pfs_session_sync(pfs_session *s)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    CK(cudaStreamSynchronize(s->st));
+    return PFS_OK;
+}
+
+int pfs_session_destroy(pfs_session *s)
+{
+    if (!s) return PFS_OK;
+    cudaStreamSynchronize(s->st);
+    delete s;
+    return PFS_OK;
+}
+
+// ---- kernel-level entry points -------------------------------------------------------------
+
+int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *p_prev, int vx, int vy, int ld,
+                        int levels, int fused, int chunk_rows, void *stream)
+{
+    if (!p_in || !b || !p_out) return fail(PFS_ERR_INVALID_ARGUMENT, "null plane");
+    if (vx <= 0 || vy <= 0 || ld < vx) return fail(PFS_ERR_INVALID_ARGUMENT, "bad dims");
+    if (levels < 1) return fail(PFS_ERR_INVALID_ARGUMENT, "levels must be >= 1");
+    if (p_in == p_out || (p_prev && (p_prev == p_in || p_prev == p_out)))
+        return fail(PFS_ERR_INVALID_ARGUMENT, "planes must be distinct");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (fused) {
+        if (vx % 4 || ld % 4 || ((uintptr_t)p_in | (uintptr_t)b | (uintptr_t)p_out | (uintptr_t)p_prev) % 16)
+            return fail(PFS_ERR_UNSUPPORTED, "fused sweeps need vx %% 4 == 0, ld %% 4 == 0, 16-byte planes");
+        if (levels > 8) return fail(PFS_ERR_UNSUPPORTED, "fused sweeps: at most 8 levels per call");
+        const int halo = levels <= 4 ? 4 : 8;
+        CK(pfs::launch_sweep_stream(p_in, b, p_out, p_prev, ld, vx, vy, levels, halo,
+                                    chunk_rows > 0 ? chunk_rows : 32, st));
+        return PFS_OK;
+    }
+    if (levels > 1 && !p_prev) return fail(PFS_ERR_INVALID_ARGUMENT, "unfused multi-sweep needs p_prev as scratch");
+    // ping-pong so that the last sweep lands in p_out and the one before in p_prev
+    const float *src = p_in;
+    for (int k = 0; k < levels; ++k) {
+        float *dst = ((levels - 1 - k) % 2 == 0) ? p_out : p_prev;
+        CK(pfs::launch_sweep_single(src, b, dst, ld, vx, vy, st));
+        src = dst;
+    }
+    return PFS_OK;
+}
+
+int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, double *rr, double *bb, void *stream)
+{
+    if (!p || !b || !rr || !bb) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
+    if (vx <= 0 || vy <= 0 || ld < vx) return fail(PFS_ERR_INVALID_ARGUMENT, "bad dims");
+    std::lock_guard<std::mutex> lk(g_mu);
+    Workspace *ws;
+    CKS(get_workspace(vx, vy, &ws));
+    cudaStream_t st = (cudaStream_t)stream;
+    Field &f = ws->f;
+    CK(pfs::launch_norms(p, b, ld, vx, vy, f.red, st));
+    CK(cudaMemcpyAsync(f.hres, f.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *rr = f.hres[0];
+    *bb = f.hres[1];
+    return PFS_OK;
+}
+
+}  // extern "C"

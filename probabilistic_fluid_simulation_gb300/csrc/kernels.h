@@ -1,0 +1,66 @@
+// Launchers of the device kernels (private to the library; the public
+// surface is include/pfs.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pfs {
+
+// Reduction scratch: one double pair per block plus a ticket, so the last
+// block sums the partials in block order (deterministic result).
+struct Reduce {
+    double *partials;   // [2 * nblocks]
+    unsigned *ticket;   // one counter, zero between launches
+    double *result;     // [2]: sum r^2 (or b^2), second slot for the paired sum
+    int nblocks;
+};
+
+constexpr int kReduceBlocks = 608;  // 4 x 152 SMs
+
+// ---- velocity / image / layout (step_kernels.cu) ----
+cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h, float dt,
+                          cudaStream_t st);
+cudaError_t launch_diffuse_sweep(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h,
+                                 float alpha, float beta, cudaStream_t st);
+// b = gamma * ((u[i+1]-u[i-1]) + (v[j+1]-v[j-1])); sum b^2 into red.result[1]
+cudaError_t launch_divergence(const float *u, const float *v, float *b, int ld, int w, int h, float gamma,
+                              const Reduce &red, cudaStream_t st);
+cudaError_t launch_project(const float *u, const float *v, const float *p, float *uo, float *vo, int ld, int w,
+                           int h, float dt, cudaStream_t st);
+// projection fused with image advection when the image grid equals the velocity grid
+cudaError_t launch_project_advect_image(const float *u, const float *v, const float *p, float *uo, float *vo,
+                                        int ld, int w, int h, float dt, const float *img, float *imgo,
+                                        size_t img_plane, int c, cudaStream_t st);
+// image advection, planar image (c planes of img_plane floats, row pitch ild), planar velocity
+cudaError_t launch_advect_image_planar(const float *img, float *imgo, size_t img_plane, int ild, int iw, int ih,
+                                       int c, const float *u, const float *v, int vld, int vw, int vh, float dt,
+                                       cudaStream_t st);
+// image advection on the reference's interleaved layout (image HWC with c
+// channels, velocity HWC with 4 channels)
+cudaError_t launch_advect_image_interleaved(const float *img, float *imgo, int iw, int ih, int c,
+                                            const float *vel, int vw, int vh, float dt, cudaStream_t st);
+// interleaved (h, w, 4) <-> planar
+cudaError_t launch_split_velocity(const float *vp, float *u, float *v, int ld, int w, int h, cudaStream_t st);
+cudaError_t launch_split_channel(const float *buf, int ch, int nch, float *plane, int ld, int w, int h,
+                                 cudaStream_t st);
+cudaError_t launch_merge_velocity(float *out, const float *u, const float *v, const float *p, const float *b,
+                                  int ld, int w, int h, cudaStream_t st);
+cudaError_t launch_split_image(const float *img, float *planes, size_t plane, int ld, int w, int h, int c,
+                               cudaStream_t st);
+cudaError_t launch_merge_image(float *img, const float *planes, size_t plane, int ld, int w, int h, int c,
+                               cudaStream_t st);
+
+// ---- pressure (sweep_kernels.cu, residual_kernels.cu) ----
+int stream_strip_width(int halo);
+cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, int ld, int w, int h,
+                                cudaStream_t st);
+cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
+                                int h, int levels, int halo, int chunk, cudaStream_t st);
+// sum over cells of r^2, r = ((((b + pL) + pR) + pT) + pB) - 4p in double, into red.result[0]
+cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
+                            cudaStream_t st);
+// both sums in one pass: r^2 into red.result[0], b^2 into red.result[1]
+cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, const Reduce &red, cudaStream_t st);
+
+}  // namespace pfs

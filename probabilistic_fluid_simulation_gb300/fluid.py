@@ -1,0 +1,274 @@
+"""Python mirror of the reference's step API over libpfs_gb300.so (include/pfs.h).
+
+The reference exposes two calls (includes/fluid.hpp:106-119):
+
+    simulate_fluid_step(vp, tmp, dt, viscosity)
+    advect_color_step(image, itmp, vp, dt)
+
+Both take the interleaved HWC buffers of src/fluid.cpp:15-17 and swap the
+caller's buffers the way the reference swaps its pointers. The functions
+here take torch CUDA tensors (device buffers, the CUDA branch of the header)
+or numpy arrays (host buffers, the CPU branch, computed on the GPU) and
+return the buffers in their new roles.
+
+`Session` keeps one simulation resident on the device in planar layout and
+advances it many steps per call (fixed sweep count or residual stop).
+
+There is no CPU fallback: if the CUDA library cannot be loaded every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional, Tuple
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libpfs_gb300.so")
+
+PFS_HOST, PFS_DEVICE = 0, 1
+
+
+class PFSError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+class _VpField(C.Structure):
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int), ("data", C.c_void_p)]
+
+
+class Params(C.Structure):
+    """pfs_params (include/pfs.h)."""
+    _fields_ = [("dt", C.c_float), ("viscosity", C.c_float), ("diffuse_iters", C.c_int), ("max_iters", C.c_int),
+                ("tol", C.c_double), ("check_every", C.c_int), ("fuse_depth", C.c_int), ("chunk_rows", C.c_int),
+                ("want_residual", C.c_int)]
+
+
+class Stats(C.Structure):
+    """pfs_stats (include/pfs.h)."""
+    _fields_ = [("sweeps", C.c_int), ("checks", C.c_int), ("rel_residual", C.c_double), ("bnorm", C.c_double),
+                ("capped", C.c_int), ("steps", C.c_longlong), ("total_sweeps", C.c_longlong),
+                ("cap_hits", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+# (name, restype, argtypes) of every symbol include/pfs.h declares
+_PP = C.POINTER(C.c_void_p)
+SIGNATURES = [
+    ("pfs_status_string", C.c_char_p, [C.c_int]),
+    ("pfs_last_error", C.c_char_p, []),
+    ("pfs_version", C.c_int, []),
+    ("pfs_set_jacobi_iters", C.c_int, [C.c_int]),
+    ("pfs_get_jacobi_iters", C.c_int, []),
+    ("pfs_set_stream", C.c_int, [C.c_void_p]),
+    ("pfs_release_workspace", C.c_int, []),
+    ("pfs_simulate_fluid_step", C.c_int, [_PP, _PP, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int]),
+    ("pfs_advect_color_step", C.c_int, [_PP, _PP, _PP, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_int]),
+    ("pfs_simulate_fluid_step_host", C.c_int, [C.POINTER(_VpField), C.POINTER(_VpField), C.c_float, C.c_float]),
+    ("pfs_advect_color_step_host", C.c_int, [C.POINTER(_VpField), C.POINTER(_VpField), C.POINTER(_VpField),
+                                             C.c_float]),
+    ("pfs_params_default", None, [C.POINTER(Params)]),
+    ("pfs_session_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(Params), C.c_void_p]),
+    ("pfs_session_set_params", C.c_int, [C.c_void_p, C.POINTER(Params)]),
+    ("pfs_session_upload", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    ("pfs_session_step", C.c_int, [C.c_void_p, C.c_int]),
+    ("pfs_session_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    ("pfs_session_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    ("pfs_session_sync", C.c_int, [C.c_void_p]),
+    ("pfs_session_destroy", C.c_int, [C.c_void_p]),
+    ("pfs_pressure_sweeps", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                      C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("pfs_residual_norms", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.c_void_p]),
+]
+
+
+def lib():
+    """Load libpfs_gb300.so (built by probabilistic_fluid_simulation_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with "
+                              "`python -m probabilistic_fluid_simulation_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int):
+    if status != 0:
+        raise PFSError(status, lib().pfs_last_error().decode())
+
+
+def set_jacobi_iters(n: int):
+    """Runtime replacement of NUM_JACOBI_ITERS (includes/fluid.hpp:11)."""
+    _check(lib().pfs_set_jacobi_iters(int(n)))
+
+
+def get_jacobi_iters() -> int:
+    return lib().pfs_get_jacobi_iters()
+
+
+def set_stream(stream_handle: int):
+    _check(lib().pfs_set_stream(C.c_void_p(stream_handle or None)))
+
+
+def _ptr(t) -> int:
+    """Device or host address of a torch tensor / numpy array (C-contiguous)."""
+    if isinstance(t, np.ndarray):
+        if not t.flags.c_contiguous or t.dtype != np.float32:
+            raise ValueError("numpy buffers must be C-contiguous float32")
+        return t.ctypes.data
+    if not t.is_contiguous() or str(t.dtype) != "torch.float32":
+        raise ValueError("tensors must be contiguous float32")
+    return t.data_ptr()
+
+
+def _pick(addr: int, *bufs):
+    for b in bufs:
+        if _ptr(b) == addr:
+            return b
+    raise RuntimeError("library returned an unknown buffer")
+
+
+def simulate_fluid_step(vp, tmp, dt: float, viscosity: float):
+    """One timestep; replaces simulate_fluid_step (includes/fluid.hpp:107/109).
+
+    vp, tmp: (h, w, 4) float32 torch CUDA tensors (device path) or numpy
+    arrays (host path). Returns (vp, tmp) in the roles the reference's
+    pointer swaps leave them."""
+    if isinstance(vp, np.ndarray):
+        h, w, z = vp.shape
+        a = _VpField(w, h, z, _ptr(vp))
+        b = _VpField(w, h, z, _ptr(tmp))
+        _check(lib().pfs_simulate_fluid_step_host(C.byref(a), C.byref(b), float(dt), float(viscosity)))
+        return _pick(a.data, vp, tmp), _pick(b.data, vp, tmp)
+    h, w, z = vp.shape
+    pa = C.c_void_p(_ptr(vp))
+    pb = C.c_void_p(_ptr(tmp))
+    _check(lib().pfs_simulate_fluid_step(C.byref(pa), C.byref(pb), float(dt), float(viscosity), w, h, z))
+    return _pick(pa.value, vp, tmp), _pick(pb.value, vp, tmp)
+
+
+def advect_color_step(image, itmp, vp, dt: float):
+    """Image advection then buffer swap; replaces advect_color_step
+    (includes/fluid.hpp:116/118). Returns (image, itmp) after the swap."""
+    ih, iw, iz = image.shape
+    vh, vw, vz = vp.shape
+    if isinstance(image, np.ndarray):
+        a = _VpField(iw, ih, iz, _ptr(image))
+        b = _VpField(iw, ih, iz, _ptr(itmp))
+        v = _VpField(vw, vh, vz, _ptr(vp))
+        _check(lib().pfs_advect_color_step_host(C.byref(a), C.byref(b), C.byref(v), float(dt)))
+        return _pick(a.data, image, itmp), _pick(b.data, image, itmp)
+    pi = C.c_void_p(_ptr(image))
+    pt = C.c_void_p(_ptr(itmp))
+    pv = C.c_void_p(_ptr(vp))
+    _check(lib().pfs_advect_color_step(C.byref(pi), C.byref(pt), C.byref(pv), float(dt), iw, ih, iz, vw, vh, vz))
+    return _pick(pi.value, image, itmp), _pick(pt.value, image, itmp)
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().pfs_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+class Session:
+    """One simulation resident on the device (pfs_session_* in include/pfs.h)."""
+
+    def __init__(self, w: int, h: int, image_shape: Optional[Tuple[int, int, int]] = None,
+                 params: Optional[Params] = None, stream: int = 0, **kw):
+        self._h = C.c_void_p()
+        self.w, self.h = w, h
+        ih, iw, ic = image_shape if image_shape else (0, 0, 0)
+        self.image_shape = (ih, iw, ic)
+        self.params = params if params is not None else default_params(**kw)
+        _check(lib().pfs_session_create(C.byref(self._h), w, h, iw, ih, ic, C.byref(self.params),
+                                        C.c_void_p(stream or None)))
+
+    def set_params(self, **kw):
+        for k, v in kw.items():
+            setattr(self.params, k, v)
+        _check(lib().pfs_session_set_params(self._h, C.byref(self.params)))
+
+    def upload(self, vp, tmp, image=None):
+        where = PFS_HOST if isinstance(vp, np.ndarray) else PFS_DEVICE
+        _check(lib().pfs_session_upload(self._h, C.c_void_p(_ptr(vp)), C.c_void_p(_ptr(tmp)),
+                                        C.c_void_p(_ptr(image) if image is not None else None), where))
+
+    def step(self, n: int = 1):
+        _check(lib().pfs_session_step(self._h, int(n)))
+
+    def download(self, vp=None, tmp=None, image=None):
+        """Fill the given buffers (numpy -> host, torch -> device); returns them."""
+        ref = next(x for x in (vp, tmp, image) if x is not None)
+        where = PFS_HOST if isinstance(ref, np.ndarray) else PFS_DEVICE
+        _check(lib().pfs_session_download(self._h, C.c_void_p(_ptr(vp) if vp is not None else None),
+                                          C.c_void_p(_ptr(tmp) if tmp is not None else None),
+                                          C.c_void_p(_ptr(image) if image is not None else None), where))
+        return vp, tmp, image
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(lib().pfs_session_stats(self._h, C.byref(s)))
+        return s.as_dict()
+
+    def sync(self):
+        _check(lib().pfs_session_sync(self._h))
+
+    def close(self):
+        if self._h:
+            lib().pfs_session_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def pressure_sweeps(p_in, b, p_out, p_prev, levels: int, fused: bool = True, chunk_rows: int = 0,
+                    w: Optional[int] = None, stream: int = 0):
+    """`levels` Jacobi sweeps on planar (h, ld) tensors whose first w columns
+    are the grid (kernel-level entry point)."""
+    h, ldd = p_in.shape
+    w = w if w is not None else ldd
+    _check(lib().pfs_pressure_sweeps(C.c_void_p(_ptr(p_in)), C.c_void_p(_ptr(b)), C.c_void_p(_ptr(p_out)),
+                                     C.c_void_p(_ptr(p_prev) if p_prev is not None else None), w, h, ldd,
+                                     int(levels), int(fused), int(chunk_rows), C.c_void_p(stream or None)))
+
+
+def residual_norms(p, b, w: Optional[int] = None, stream: int = 0) -> Tuple[float, float]:
+    """(||b - A p||^2, ||b||^2) in FP64 for planar (h, ld) tensors."""
+    h, ld = p.shape
+    rr, bb = C.c_double(), C.c_double()
+    _check(lib().pfs_residual_norms(C.c_void_p(_ptr(p)), C.c_void_p(_ptr(b)), w or ld, h, ld, C.byref(rr),
+                                    C.byref(bb), C.c_void_p(stream or None)))
+    return rr.value, bb.value
