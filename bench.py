@@ -1,0 +1,362 @@
+"""Benchmark of the per-timestep fluid update on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one full timestep of the simulation (src/fluid.cpp:298-320 and
+src/main.cpp:236-239): velocity advection, divergence, the pressure Jacobi
+iteration to relative residual 1e-5 (FP64-checked every 100 sweeps, capped at
+2000 sweeps), projection and 3-channel image advection, on a 2048x2048 float32
+grid with dt = 0.05 and synthetic seeded inputs (8 Gaussian vortices, 16
+Gaussian blobs). Fields stay resident in HBM between steps (a session).
+
+Printed (rank 0, one JSON line): cell-updates/s for the whole job; e2e, the
+same metric through the C ABI with pinned host buffers copied in and out
+every step; the roofline of the dominant kernel (the fused pressure sweep);
+a CPU baseline (the oracle port on this host's cores, bounded sample); the
+SM clocks sampled during the timed region; kernel launches in the timed
+region.
+
+--impl reference times the reference algorithm on the host cores instead
+(the oracle port; the reference's own build cannot be compiled on the GPU
+host because its sources are not there) and prints the same line with
+"impl": "reference".
+
+Several GPUs (torchrun): one independent simulation per rank (seed 1 + rank),
+no data exchange; the value is the sum over ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s to residual 1e-5: mixed/batched/warm-start vs plain FP32, 1 GB300"
+UNIT = "cell-updates/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "sweep_stream_traffic.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--channels", type=int, default=3)
+    ap.add_argument("--dt", type=float, default=0.05)
+    ap.add_argument("--tol", type=float, default=1e-5)
+    ap.add_argument("--cap", type=int, default=2000)
+    ap.add_argument("--check-every", type=int, default=100)
+    ap.add_argument("--diffuse-iters", type=int, default=40)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--fuse-depth", type=int, default=0)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--ref-budget-s", type=float, default=90.0)
+    return ap.parse_args()
+
+
+def workload(a):
+    return (f"{a.size}x{a.size} f32 grid, dt {a.dt}, pressure Jacobi to relative residual {a.tol:g} "
+            f"(FP64 check every {a.check_every} sweeps, cap {a.cap}), {a.channels}-channel image, "
+            f"viscosity 0 ({a.diffuse_iters} identity diffusion sweeps), {a.steps} steps")
+
+
+def config(a, extra=None):
+    cells = a.size * a.size
+    state_mb = cells * 4 * (8 + 2 * a.channels) / 1e6
+    c = {"workload": workload(a), "grid": [a.size, a.size], "image_channels": a.channels, "dt": a.dt,
+         "tol": a.tol, "max_iters": a.cap, "check_every": a.check_every, "seed": a.seed, "form": "plain-fp32",
+         "l2": f"per-step state {state_mb:.0f} MB > 129 MB L2; no flush between steps"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+DATA = "synthetic (seeded Gaussian vortices and blobs; the reference's PNG inputs are not used)"
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_launch(cells, levels):
+    """DRAM bytes per fused-sweep launch from the committed ncu summary (scaled
+    by cells when the capture used a smaller grid), or None."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            t = json.load(f)
+    except (OSError, ValueError):
+        return None, None
+    if t.get("levels") != levels:
+        return None, None
+    return t["dram_bytes_per_launch"] * cells / t["cells"], t.get("source")
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU side (the oracle port of src/fluid.cpp): our arm's cpu_baseline and the reference arm
+
+def cpu_run(a, steps, warmup=0, budget_s=None):
+    from oracle import oracle as O
+    from probabilistic_fluid_simulation_gb300 import synthetic
+    threads = O.set_threads(os.cpu_count() or 1)
+    vp, tmp, img, itmp = synthetic.initial_state(a.size, a.size, a.channels, a.seed)
+
+    def one():
+        nonlocal vp, tmp, img, itmp
+        vp, tmp, st = O.step(vp, tmp, a.dt, 0.0, diffuse_iters=a.diffuse_iters, max_iters=a.cap, tol=a.tol,
+                             check_every=a.check_every)
+        img, itmp = O.advect_color_step(img, itmp, vp, a.dt)
+        return st
+
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    done = 0
+    sweeps = []
+    while done < steps:
+        sweeps.append(one().sweeps)
+        done += 1
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return a.size * a.size * done / el, done, el, threads, sweeps
+
+
+def reference_arm(a, rank):
+    if rank != 0:
+        return 0
+    w = min(a.warmup, 1)
+    val, done, el, threads, sweeps = cpu_run(a, a.steps, warmup=w, budget_s=a.ref_budget_s)
+    sample = (f"{done} of {a.steps} requested steps timed (time budget {a.ref_budget_s:.0f} s), {w} untimed; "
+              f"full {a.size}x{a.size} workload, {int(np.mean(sweeps))} sweeps/step")
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": a.gpus, "steps": done,
+            "warmup": w, "ms_per_step": 1e3 * el / done, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": config(a, {"runs_on": f"host CPU, {threads} threads (oracle port of src/fluid.cpp)"}),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------------------------
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        return reference_arm(a, rank)
+
+    import torch
+    from probabilistic_fluid_simulation_gb300 import fluid, synthetic
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    cells = a.size * a.size
+    vp, tmp, img, itmp = synthetic.initial_state(a.size, a.size, a.channels, a.seed + rank)
+    params = fluid.default_params(dt=a.dt, viscosity=0.0, diffuse_iters=a.diffuse_iters, max_iters=a.cap,
+                                  tol=a.tol, check_every=a.check_every, fuse_depth=a.fuse_depth,
+                                  chunk_rows=a.chunk)
+    sess = fluid.Session(a.size, a.size, image_shape=img.shape, params=params, stream=stream)
+    sess.upload(vp, tmp, img)
+
+    for _ in range(a.warmup):
+        sess.step(1)
+    sess.sync()
+    st0 = sess.stats()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)  # let the sampler come up
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = fluid.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    sweeps = []
+    for _ in range(a.steps):
+        sess.step(1)
+        sweeps.append(sess.stats()["sweeps"])
+    ev1.record()
+    torch.cuda.synchronize()
+    launches = fluid.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    clk = clocks.stop()
+    st1 = sess.stats()
+    value = cells * a.steps * world / (ms / 1e3)
+
+    # Dominant kernel: the fused pressure sweep, timed alone on this stream.
+    levels = a.fuse_depth or 8
+    chunk = a.chunk or 32
+    ld = (a.size + 31) // 32 * 32
+    p = torch.randn(a.size, ld, device="cuda")
+    bpl = torch.randn(a.size, ld, device="cuda")
+    q = torch.empty_like(p)
+    for _ in range(5):
+        fluid.pressure_sweeps(p, bpl, q, None, levels, fused=True, chunk_rows=chunk, w=a.size, stream=stream)
+    nrep = 200
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    k0.record()
+    for i in range(nrep):
+        src, dst = (p, q) if i % 2 == 0 else (q, p)
+        fluid.pressure_sweeps(src, bpl, dst, None, levels, fused=True, chunk_rows=chunk, w=a.size, stream=stream)
+    k1.record()
+    torch.cuda.synchronize()
+    kms = k0.elapsed_time(k1) / nrep
+    peak, peak_src = measured_peak()
+    alg_bytes = 12.0 * cells * levels
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    traffic, tsrc = traffic_per_launch(cells, levels)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": f"k_sweep_stream<8,{levels}>", "levels_per_launch": levels,
+                "avg_launch_us": kms * 1e3, "algorithmic_bytes_per_launch": alg_bytes,
+                "peak_source": f"{peak_src} (hbm_gbs, burst copy)",
+                "note": "algorithmic bytes = 12 B per cell per sweep (read p, b; write p) x sweeps fused per "
+                        "launch; the fused launch reads and writes each plane once, so frac > 1 is the "
+                        "temporal-blocking gain, and traffic (ncu DRAM bytes) shows the bytes actually moved",
+                "traffic_source": tsrc}
+    del p, bpl, q
+
+    # e2e: the same steps through the C ABI with pinned host buffers in and out each step
+    e2e = None
+    if not a.no_e2e:
+        ne = a.e2e_steps or a.steps
+        hv = torch.from_numpy(vp.copy()).pin_memory().numpy()
+        ht = torch.from_numpy(np.zeros_like(tmp)).pin_memory().numpy()
+        hi = torch.from_numpy(img.copy()).pin_memory().numpy()
+        sess.upload(hv, ht, hi)
+        sess.step(1)
+        sess.download(hv, ht, hi)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            sess.upload(hv, ht, hi)
+            sess.step(1)
+            sess.download(hv, ht, hi)
+        el = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([el], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        nbytes = hv.nbytes + ht.nbytes + hi.nbytes
+        e2e = {"value": cells * ne * world / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "steps": ne,
+               "api": "pfs_session_upload(PFS_HOST) + pfs_session_step(1) + pfs_session_download(PFS_HOST)"}
+    sess.close()
+
+    cpu = None
+    if rank == 0 and not a.no_cpu and a.cpu_steps > 0:
+        val, done, el, threads, cs = cpu_run(a, a.cpu_steps)
+        cpu = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{done} full {a.size}x{a.size} steps of the same workload ({int(np.mean(cs))} "
+                         f"sweeps/step), oracle port of src/fluid.cpp, {el:.1f} s"}
+
+    if rank == 0:
+        mean_sweeps = float(np.mean(sweeps))
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": DATA,
+                "config": config(a, {"fuse_depth": levels, "chunk_rows": chunk}),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk,
+                "solver": {"sweeps_per_step": mean_sweeps, "cap_hits": st1["cap_hits"] - st0["cap_hits"],
+                           "final_rel_residual": st1["rel_residual"],
+                           "cell_sweeps_per_s": cells * mean_sweeps * a.steps * world / (ms / 1e3)}}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

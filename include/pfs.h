@@ -55,6 +55,8 @@ const char *pfs_status_string(int status);
 const char *pfs_last_error(void);
 /* Library version as 10000*major + 100*minor + patch. */
 int pfs_version(void);
+/* Number of CUDA kernels this library has launched since it was loaded. */
+long long pfs_kernel_launches(void);
 
 /* ---- global settings --------------------------------------------------------- */
 /* Sweep count of both diffusion and pressure per step; replaces

@@ -26,6 +26,10 @@
 
 using pfs::Reduce;
 
+namespace pfs {
+std::atomic<long long> g_launches{0};
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -299,6 +303,14 @@ int check_dims(int vx, int vy, int vz, float dt)
     return PFS_OK;
 }
 
+// The interleaved velocity kernels move one cell as a float4.
+int check_aligned(const void *p, const char *what)
+{
+    if (((uintptr_t)p) % 16 != 0)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "%s must be 16-byte aligned (cudaMalloc pointers are)", what);
+    return PFS_OK;
+}
+
 StepCfg dropin_cfg(float dt, float visc)
 {
     StepCfg c;
@@ -380,6 +392,8 @@ const char *pfs_last_error(void) { return g_err.c_str(); }
 
 int pfs_version(void) { return 100; }
 
+long long pfs_kernel_launches(void) { return pfs::g_launches.load(std::memory_order_relaxed); }
+
 int pfs_set_jacobi_iters(int n)
 {
     if (n < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "sweep count must be >= 0");
@@ -421,6 +435,8 @@ int pfs_simulate_fluid_step(float **vp, float **tmp, float dt, float viscosity, 
     if (*vp == *tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "vp and tmp must be distinct buffers");
     CKS(check_dims(vx, vy, vz, dt));
     if (!std::isfinite(viscosity)) return fail(PFS_ERR_NOT_FINITE, "viscosity must be finite");
+    CKS(check_aligned(*vp, "vp"));
+    CKS(check_aligned(*tmp, "tmp"));
     std::lock_guard<std::mutex> lk(g_mu);
     return dropin_step(*vp, *tmp, vx, vy, dt, viscosity, g_stream);
 }
@@ -432,6 +448,7 @@ int pfs_advect_color_step(float **image, float **itmp, float **vp, float dt, int
     if (*image == *itmp) return fail(PFS_ERR_INVALID_ARGUMENT, "image and itmp must be distinct buffers");
     if (ix <= 0 || iy <= 0 || iz <= 0) return fail(PFS_ERR_INVALID_ARGUMENT, "bad image dims");
     CKS(check_dims(vx, vy, vz, dt));
+    CKS(check_aligned(*vp, "vp"));
     cudaStream_t st;
     {
         std::lock_guard<std::mutex> lk(g_mu);
@@ -626,6 +643,9 @@ int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const 
         I = dI;
     } else if (where != PFS_DEVICE) {
         return fail(PFS_ERR_INVALID_ARGUMENT, "where must be PFS_HOST or PFS_DEVICE");
+    } else {
+        CKS(check_aligned(vp, "vp"));
+        CKS(check_aligned(tmp, "tmp"));
     }
     f.pidx[0] = 0;
     f.pidx[1] = 1;
@@ -695,6 +715,9 @@ int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, in
         I = (image && icount) ? s->stage + 2 * vcount : nullptr;
     } else if (where != PFS_DEVICE) {
         return fail(PFS_ERR_INVALID_ARGUMENT, "where must be PFS_HOST or PFS_DEVICE");
+    } else {
+        if (vp) CKS(check_aligned(vp, "vp"));
+        if (tmp) CKS(check_aligned(tmp, "tmp"));
     }
     const int W = s->vpSlot, Z = s->tmpSlot;
     if (A) CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, f.w, f.h, s->st));

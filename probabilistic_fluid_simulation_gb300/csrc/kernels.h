@@ -5,13 +5,23 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace pfs {
+
+// Kernels launched by this library since it was loaded (pfs_kernel_launches()).
+extern std::atomic<long long> g_launches;
+inline cudaError_t launched(int n = 1)
+{
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+    return cudaGetLastError();
+}
 
 // Reduction scratch: one double pair per block plus a ticket, so the last
 // block sums the partials in block order (deterministic result).
 struct Reduce {
     double *partials;   // [2 * nblocks]
-    unsigned *ticket;   // one counter, zero between launches
+    unsigned *ticket;   // one counter per result slot, zero between launches
     double *result;     // [2]: sum r^2 (or b^2), second slot for the paired sum
     int nblocks;
 };

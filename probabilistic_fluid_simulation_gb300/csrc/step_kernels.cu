@@ -66,7 +66,8 @@ __global__ void k_diffuse(const float *__restrict__ u, const float *__restrict__
 
 // Block sum of `acc`, written to red.partials[blockIdx.x * 2 + slot]; the last
 // block to finish adds the partials in block order into red.result[slot] and
-// re-arms the ticket. The order of additions is fixed, so the sum is
+// re-arms that slot's ticket (one ticket per slot, so two reductions in one
+// kernel do not mix their counts). The order of additions is fixed, so the sum is
 // reproducible run to run.
 __device__ void reduce_blocks(double acc, const Reduce &red, int slot)
 {
@@ -84,7 +85,7 @@ __device__ void reduce_blocks(double acc, const Reduce &red, int slot)
         if (lane == 0) {
             red.partials[blockIdx.x * 2 + slot] = acc;
             __threadfence();
-            last = atomicAdd(red.ticket, 1u) == gridDim.x - 1;
+            last = atomicAdd(red.ticket + slot, 1u) == gridDim.x - 1;
         }
     }
     __syncthreads();
@@ -96,7 +97,7 @@ __device__ void reduce_blocks(double acc, const Reduce &red, int slot)
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0) {
             red.result[slot] = s;
-            *red.ticket = 0u;
+            red.ticket[slot] = 0u;
         }
     }
 }
@@ -297,41 +298,41 @@ cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, 
                           cudaStream_t st)
 {
     k_advect<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, uo, vo, ld, w, h, dt);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_diffuse_sweep(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h,
                                  float alpha, float beta, cudaStream_t st)
 {
     k_diffuse<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, uo, vo, ld, w, h, alpha, beta);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_divergence(const float *u, const float *v, float *b, int ld, int w, int h, float gamma,
                               const Reduce &red, cudaStream_t st)
 {
     k_divergence<<<red.nblocks, 256, 0, st>>>(u, v, b, ld, w, h, gamma, red);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
                             cudaStream_t st)
 {
     k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, const Reduce &red, cudaStream_t st)
 {
     k_norms<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_project(const float *u, const float *v, const float *p, float *uo, float *vo, int ld, int w,
                            int h, float dt, cudaStream_t st)
 {
     k_project<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, p, uo, vo, ld, w, h, dt);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_project_advect_image(const float *u, const float *v, const float *p, float *uo, float *vo,
@@ -340,7 +341,7 @@ cudaError_t launch_project_advect_image(const float *u, const float *v, const fl
 {
     k_project_advect_image<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, p, uo, vo, ld, w, h, dt, img, imgo,
                                                                      img_plane, c);
-    return cudaGetLastError();
+    return launched();
 }
 
 // viw = fvw/fiw, kx = dt/viw exactly as src/fluid.cpp:82-83,97 compute them.
@@ -360,7 +361,7 @@ cudaError_t launch_advect_image_planar(const float *img, float *imgo, size_t img
     image_scales(iw, ih, vw, vh, dt, viw, vih, kx, ky);
     k_advect_image_planar<<<grid2d(iw, ih), dim3(kBX, kBY), 0, st>>>(img, imgo, img_plane, ild, iw, ih, c, u, v, vld,
                                                                      vw, vh, dt, viw, vih, kx, ky);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_advect_image_interleaved(const float *img, float *imgo, int iw, int ih, int c,
@@ -370,41 +371,41 @@ cudaError_t launch_advect_image_interleaved(const float *img, float *imgo, int i
     image_scales(iw, ih, vw, vh, dt, viw, vih, kx, ky);
     k_advect_image_interleaved<<<grid2d(iw, ih), dim3(kBX, kBY), 0, st>>>(img, imgo, iw, ih, c, vel, vw, vh, dt,
                                                                            viw, vih, kx, ky);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_split_velocity(const float *vp, float *u, float *v, int ld, int w, int h, cudaStream_t st)
 {
     k_split_velocity<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(reinterpret_cast<const float4 *>(vp), u, v, ld, w, h);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_split_channel(const float *buf, int ch, int nch, float *plane, int ld, int w, int h,
                                  cudaStream_t st)
 {
     k_split_channel<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(buf, ch, nch, plane, ld, w, h);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_merge_velocity(float *out, const float *u, const float *v, const float *p, const float *b,
                                   int ld, int w, int h, cudaStream_t st)
 {
     k_merge_velocity<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(reinterpret_cast<float4 *>(out), u, v, p, b, ld, w, h);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_split_image(const float *img, float *planes, size_t plane, int ld, int w, int h, int c,
                                cudaStream_t st)
 {
     k_split_image<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(img, planes, plane, ld, w, h, c);
-    return cudaGetLastError();
+    return launched();
 }
 
 cudaError_t launch_merge_image(float *img, const float *planes, size_t plane, int ld, int w, int h, int c,
                                cudaStream_t st)
 {
     k_merge_image<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(img, planes, plane, ld, w, h, c);
-    return cudaGetLastError();
+    return launched();
 }
 
 }  // namespace pfs

@@ -141,7 +141,7 @@ cudaError_t launch_stream_t(const StreamArgs &a, cudaStream_t st)
 {
     const int blocks = (a.nwork + 3) / 4;
     k_sweep_stream<G, L, PREV><<<blocks, 128, 0, st>>>(a);
-    return cudaGetLastError();
+    return launched();
 }
 
 template <int G, int L>
@@ -160,7 +160,7 @@ cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, i
     dim3 blk(32, 8);
     dim3 grd((w + 31) / 32, (h + 7) / 8);
     k_sweep_single<<<grd, blk, 0, st>>>(pin, b, pout, ld, w, h);
-    return cudaGetLastError();
+    return launched();
 }
 
 // levels in [1, halo]; halo in {4, 8}; w % 4 == 0; ld % 4 == 0; 16-byte aligned planes.

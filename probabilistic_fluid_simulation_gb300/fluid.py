@@ -67,6 +67,7 @@ SIGNATURES = [
     ("pfs_status_string", C.c_char_p, [C.c_int]),
     ("pfs_last_error", C.c_char_p, []),
     ("pfs_version", C.c_int, []),
+    ("pfs_kernel_launches", C.c_longlong, []),
     ("pfs_set_jacobi_iters", C.c_int, [C.c_int]),
     ("pfs_get_jacobi_iters", C.c_int, []),
     ("pfs_set_stream", C.c_int, [C.c_void_p]),
@@ -122,6 +123,11 @@ def set_jacobi_iters(n: int):
 
 def get_jacobi_iters() -> int:
     return lib().pfs_get_jacobi_iters()
+
+
+def kernel_launches() -> int:
+    """Kernels the library has launched since it was loaded."""
+    return lib().pfs_kernel_launches()
 
 
 def set_stream(stream_handle: int):

@@ -131,18 +131,21 @@ def velocity_from_vortices(w: int, h: int, vortices: Sequence[Vortex]) -> np.nda
 
     Each vortex has stream function psi = G R e^(1/2) exp(-r^2 / 2R^2), so
     u = dpsi/dy, v = -dpsi/dx peak at |G| on the ring r = R and the field is
-    divergence-free; distances use the minimum image, so it is periodic.
+    divergence-free; distances use the minimum image, so it is periodic. The
+    Gaussian is evaluated as a product of its x and y factors.
     """
-    x = np.arange(w, dtype=np.float64)[None, :]
-    y = np.arange(h, dtype=np.float64)[:, None]
+    x = np.arange(w, dtype=np.float64)
+    y = np.arange(h, dtype=np.float64)
     u = np.zeros((h, w), np.float64)
     v = np.zeros((h, w), np.float64)
+    e05 = float(det_exp(0.5))
     for vx in vortices:
         dx = _min_image(x, vx.cx, w)
         dy = _min_image(y, vx.cy, h)
-        e = det_exp(0.5 - (dx * dx + dy * dy) / (2.0 * vx.radius * vx.radius))
-        u += -vx.circulation * (dy / vx.radius) * e
-        v += vx.circulation * (dx / vx.radius) * e
+        s2 = 2.0 * vx.radius * vx.radius
+        e = det_exp(-(dy * dy) / s2)[:, None] * (e05 * det_exp(-(dx * dx) / s2))[None, :]
+        u += (-vx.circulation / vx.radius) * dy[:, None] * e
+        v += (vx.circulation / vx.radius) * dx[None, :] * e
     out = np.zeros((h, w, 4), np.float32)
     out[..., 0] = u
     out[..., 1] = v
@@ -159,8 +162,8 @@ def blob_image(w: int, h: int, channels: int, seed: int, count: int = 16,
     """Seeded image of `count` Gaussian blobs, interleaved (h, w, C) float32 in [0, 1]."""
     rng = SplitMix64(seed ^ 0xB10B5EED)
     s = _size_scale(w, h)
-    x = np.arange(w, dtype=np.float64)[None, :]
-    y = np.arange(h, dtype=np.float64)[:, None]
+    x = np.arange(w, dtype=np.float64)
+    y = np.arange(h, dtype=np.float64)
     img = np.zeros((h, w, channels), np.float64)
     for _ in range(count):
         cx = rng.uniform(0.0, w)
@@ -169,7 +172,8 @@ def blob_image(w: int, h: int, channels: int, seed: int, count: int = 16,
         colour = [rng.uniform() for _ in range(channels)]
         dx = _min_image(x, cx, w)
         dy = _min_image(y, cy, h)
-        e = det_exp(-(dx * dx + dy * dy) / (2.0 * r * r))
+        s2 = 2.0 * r * r
+        e = det_exp(-(dy * dy) / s2)[:, None] * det_exp(-(dx * dx) / s2)[None, :]
         for k in range(channels):
             img[..., k] += colour[k] * e
     return np.clip(img, 0.0, 1.0).astype(np.float32)
