@@ -75,6 +75,8 @@ struct Field {
     double *rmem = nullptr;
     unsigned *ticket = nullptr;
     double *hres = nullptr;  // pinned, [2]
+    pfs::SolveState *dstate = nullptr;  // device
+    pfs::SolveState *hstate = nullptr;  // pinned host copy
     Reduce red{};
 
     int alloc(int w_, int h_)
@@ -102,6 +104,9 @@ struct Field {
         CK(cudaMemset(rmem, 0, (2 * nb + 2) * sizeof(double) + 16));
         ticket = reinterpret_cast<unsigned *>(rmem + 2 * nb + 2);
         CK(cudaMallocHost(&hres, 2 * sizeof(double)));
+        CK(cudaMalloc(&dstate, sizeof(pfs::SolveState)));
+        CK(cudaMemset(dstate, 0, sizeof(pfs::SolveState)));
+        CK(cudaMallocHost(&hstate, sizeof(pfs::SolveState)));
         red.partials = rmem;
         red.result = rmem + 2 * nb;
         red.ticket = ticket;
@@ -113,9 +118,13 @@ struct Field {
         if (mem) cudaFree(mem);
         if (rmem) cudaFree(rmem);
         if (hres) cudaFreeHost(hres);
+        if (dstate) cudaFree(dstate);
+        if (hstate) cudaFreeHost(hstate);
         mem = nullptr;
         rmem = nullptr;
         hres = nullptr;
+        dstate = nullptr;
+        hstate = nullptr;
         w = h = 0;
     }
     ~Field() { release(); }
@@ -147,7 +156,7 @@ bool fused_ok(const Field &f) { return f.w % 4 == 0; }
 // Sum r^2 of pressure plane `pp` and read back (r^2, b^2) (b^2 from the last divergence).
 int residual_host(Field &f, const float *pp, cudaStream_t st, double &rr, double &bb)
 {
-    CK(pfs::launch_residual(pp, f.b, f.ld, f.w, f.h, f.red, st));
+    CK(pfs::launch_residual(pp, f.b, f.ld, f.w, f.h, f.red, nullptr, 0, 0.0, st));
     CK(cudaMemcpyAsync(f.hres, f.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     rr = f.hres[0];
@@ -157,8 +166,21 @@ int residual_host(Field &f, const float *pp, cudaStream_t st, double &rr, double
 
 double relative(double rr, double bb) { return bb > 0.0 ? std::sqrt(rr) / std::sqrt(bb) : std::sqrt(rr); }
 
+// Plane roles after the launches that end at one check point.
+struct CheckPoint {
+    int sweeps, cur, prev;
+};
+
 // Pressure iteration of src/fluid.cpp:239-266 from slot X's plane (q_0) with
 // Y's plane as the other buffer. Afterwards `cur` holds q_S and `prev` q_{S-1}.
+//
+// Residual mode: the sweeps are cut at check points (multiples of
+// check_every, and the cap); after each, a residual launch evaluates the
+// relative residual on the device and raises SolveState::done once it is at
+// or below tol, which turns every later sweep and residual launch of the
+// solve into an immediate return. The host enqueues check intervals in
+// batches that double in size (1, 2, 4, ...) and reads the state only between
+// batches, then takes the plane roles recorded at the converged check point.
 int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStream_t st, int &cur, int &prev)
 {
     cur = f.pidx[X];
@@ -166,13 +188,20 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     int freep = 3 - cur - prev;
     const bool fused = fused_ok(f);
     const int L = std::max(1, std::min(c.tun.levels, c.tun.halo));
+    const bool resid = c.tol > 0.0;
+    const int *done = resid ? &f.dstate->done : nullptr;
+    if (resid) CK(cudaMemsetAsync(f.dstate, 0, sizeof(pfs::SolveState), st));
+
+    CheckPoint marks[64];
+    int nmarks = 0, batch = 1, in_batch = 0;
     int S = 0;
-    while (S < c.S) {
+    bool finished = false;
+    while (S < c.S && !finished) {
         int stop = c.S;
-        if (c.tol > 0.0 && c.check_every > 0) stop = std::min(c.S, (S / c.check_every + 1) * c.check_every);
+        if (resid && c.check_every > 0) stop = std::min(c.S, (S / c.check_every + 1) * c.check_every);
         while (S < stop) {
             if (!fused) {
-                CK(pfs::launch_sweep_single(f.p[cur], f.b, f.p[freep], f.ld, f.w, f.h, st));
+                CK(pfs::launch_sweep_single(f.p[cur], f.b, f.p[freep], f.ld, f.w, f.h, done, st));
                 const int old_prev = prev;
                 prev = cur;
                 cur = freep;
@@ -183,31 +212,44 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
             const int n = std::min(L, stop - S);
             const bool last = (S + n == stop);
             CK(pfs::launch_sweep_stream(f.p[cur], f.b, f.p[freep], last ? f.p[prev] : nullptr, f.ld, f.w, f.h, n,
-                                        c.tun.halo, c.tun.chunk, st));
-            if (last) {
-                const int old_cur = cur;
-                cur = freep;  // q_S
-                freep = old_cur;
-                // prev now holds q_{S-1}
-            } else {
-                const int old_cur = cur;
-                cur = freep;
-                freep = old_cur;
-            }
+                                        c.tun.halo, c.tun.chunk, done, st));
+            const int old_cur = cur;
+            cur = freep;  // q_S; after a `last` launch prev holds q_{S-1}
+            freep = old_cur;
             S += n;
         }
-        if (c.tol > 0.0) {
-            double rr, bb;
-            CKS(residual_host(f, f.p[cur], st, rr, bb));
-            o.checks++;
-            o.bnorm = std::sqrt(bb);
-            o.rel = relative(rr, bb);
-            if (o.rel <= c.tol) break;
+        if (!resid) break;
+        CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, st));
+        marks[nmarks++] = {S, cur, prev};
+        if (++in_batch == batch || S == c.S || nmarks == 64) {
+            CK(cudaMemcpyAsync(f.hstate, f.dstate, sizeof(pfs::SolveState), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (f.hstate->done || S == c.S) finished = true;
+            if (nmarks == 64 && !finished) {  // keep the latest mark only
+                marks[0] = marks[63];
+                nmarks = 1;
+            }
+            in_batch = 0;
+            batch = std::min(batch * 2, 16);
+        }
+    }
+    if (resid && nmarks > 0) {
+        const pfs::SolveState &hs = *f.hstate;  // copied at the last sync
+        o.checks = hs.checks;
+        o.rel = hs.rel;
+        o.bnorm = std::sqrt(hs.bb);
+        if (hs.done) {
+            int k = nmarks - 1;
+            while (k > 0 && marks[k].sweeps != hs.sweeps) --k;
+            if (marks[k].sweeps != hs.sweeps) return fail(PFS_ERR_CUDA, "lost the converged check point");
+            S = hs.sweeps;
+            cur = marks[k].cur;
+            prev = marks[k].prev;
         }
     }
     o.sweeps = S;
-    o.capped = c.tol > 0.0 && S == c.S && !(o.rel <= c.tol);
-    if (c.want_res && !(c.tol > 0.0)) {
+    o.capped = resid && S == c.S && !(o.rel <= c.tol);
+    if (c.want_res && !resid) {
         double rr, bb;
         CKS(residual_host(f, f.p[cur], st, rr, bb));
         o.bnorm = std::sqrt(bb);
@@ -772,7 +814,7 @@ int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *
         if (levels > 8) return fail(PFS_ERR_UNSUPPORTED, "fused sweeps: at most 8 levels per call");
         const int halo = levels <= 4 ? 4 : 8;
         CK(pfs::launch_sweep_stream(p_in, b, p_out, p_prev, ld, vx, vy, levels, halo,
-                                    chunk_rows > 0 ? chunk_rows : 32, st));
+                                    chunk_rows > 0 ? chunk_rows : 32, nullptr, st));
         return PFS_OK;
     }
     if (levels > 1 && !p_prev) return fail(PFS_ERR_INVALID_ARGUMENT, "unfused multi-sweep needs p_prev as scratch");
@@ -780,7 +822,7 @@ int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *
     const float *src = p_in;
     for (int k = 0; k < levels; ++k) {
         float *dst = ((levels - 1 - k) % 2 == 0) ? p_out : p_prev;
-        CK(pfs::launch_sweep_single(src, b, dst, ld, vx, vy, st));
+        CK(pfs::launch_sweep_single(src, b, dst, ld, vx, vy, nullptr, st));
         src = dst;
     }
     return PFS_OK;

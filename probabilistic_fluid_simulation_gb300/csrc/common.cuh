@@ -25,8 +25,25 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
 // Periodic wrap of a backtraced coordinate, fmod(fmod(x, n) + n, n) in float
-// (src/fluid.cpp:48-49,105-106). CUDA's fmodf is exact, like libm's.
-__device__ __forceinline__ float wrap_coord(float x, float n) { return fmodf(fadd(fmodf(x, n), n), n); }
+// (src/fluid.cpp:48-49,105-106). fmod is exact (its result is always
+// representable), so for -n <= x < 2n each fmod reduces to a comparison and
+// at most one subtraction of n, which is exact there (Sterbenz); other x take
+// CUDA's fmodf, which is exact as well. Same bits either way.
+__device__ __forceinline__ float fmod_small(float x, float n)
+{
+    // x in [-n, 2n]: fmod keeps the sign of x and |result| < n
+    if (x >= n) return x == 2.0f * n ? 0.0f : fsub(x, n);
+    if (x == -n) return -0.0f;
+    return x;
+}
+__device__ __forceinline__ float wrap_coord(float x, float n)
+{
+    if (x >= -n && x < 2.0f * n) {
+        const float y = fadd(fmod_small(x, n), n);  // in [0, 2n]
+        return fmod_small(y, n);
+    }
+    return fmodf(fadd(fmodf(x, n), n), n);
+}
 
 // Bilinear sample with the reference's weights and summation order
 // (src/fluid.cpp:62-66): ((a + b) + c) + d, each term ((1-sx)(1-sy)) f.

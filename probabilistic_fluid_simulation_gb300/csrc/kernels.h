@@ -28,6 +28,19 @@ struct Reduce {
 
 constexpr int kReduceBlocks = 608;  // 4 x 152 SMs
 
+// Device-side state of one pressure solve in residual mode. The residual
+// kernel at a check point sets `done` when ||r||/||b|| <= tol; sweep and
+// residual launches enqueued after that see the flag and return at once.
+struct SolveState {
+    int done;
+    int sweeps;  // sweep count at the check that converged
+    int checks;  // residual evaluations performed
+    int pad;
+    double rel;  // last evaluated relative residual
+    double rr;   // last evaluated sum r^2
+    double bb;   // sum b^2 of this step's divergence
+};
+
 // ---- velocity / image / layout (step_kernels.cu) ----
 cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h, float dt,
                           cudaStream_t st);
@@ -63,13 +76,17 @@ cudaError_t launch_merge_image(float *img, const float *planes, size_t plane, in
 
 // ---- pressure (sweep_kernels.cu, residual_kernels.cu) ----
 int stream_strip_width(int halo);
+// `done` (may be null): skip the launch when *done != 0
 cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, int ld, int w, int h,
-                                cudaStream_t st);
+                                const int *done, cudaStream_t st);
 cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
-                                int h, int levels, int halo, int chunk, cudaStream_t st);
-// sum over cells of r^2, r = ((((b + pL) + pR) + pT) + pB) - 4p in double, into red.result[0]
+                                int h, int levels, int halo, int chunk, const int *done, cudaStream_t st);
+// sum over cells of r^2, r = b + pL + pR + pT + pB - 4p (exact per cell), into
+// red.result[0]. With `state`: skipped when state->done; otherwise records the
+// check (rel = sqrt(r^2)/sqrt(b^2) from red.result[1]) and marks the solve
+// done at `sweeps_here` sweeps when rel <= tol.
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
-                            cudaStream_t st);
+                            SolveState *state, int sweeps_here, double tol, cudaStream_t st);
 // both sums in one pass: r^2 into red.result[0], b^2 into red.result[1]
 cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, const Reduce &red, cudaStream_t st);
 

@@ -69,7 +69,8 @@ __global__ void k_diffuse(const float *__restrict__ u, const float *__restrict__
 // re-arms that slot's ticket (one ticket per slot, so two reductions in one
 // kernel do not mix their counts). The order of additions is fixed, so the sum is
 // reproducible run to run.
-__device__ void reduce_blocks(double acc, const Reduce &red, int slot)
+__device__ void reduce_blocks(double acc, const Reduce &red, int slot, SolveState *state = nullptr,
+                              int sweeps_here = 0, double tol = 0.0)
 {
     __shared__ double ws[32];
     __shared__ bool last;
@@ -98,8 +99,58 @@ __device__ void reduce_blocks(double acc, const Reduce &red, int slot)
         if (lane == 0) {
             red.result[slot] = s;
             red.ticket[slot] = 0u;
+            if (state) {
+                const double bb = red.result[1];
+                const double rel = bb > 0.0 ? __dsqrt_rn(s) / __dsqrt_rn(bb) : __dsqrt_rn(s);
+                state->rr = s;
+                state->bb = bb;
+                state->rel = rel;
+                state->checks += 1;
+                if (rel <= tol) {
+                    state->sweeps = sweeps_here;
+                    state->done = 1;
+                }
+            }
         }
     }
+}
+
+// Error-free float transformations (Knuth's TwoSum, and the product error
+// from one fused multiply-add) used to evaluate the residual exactly without
+// FP64 arithmetic per cell: on GB300 the FP64 pipe runs at a small fraction
+// of the FP32 rate.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+// Per-thread sum of squares kept as an unevaluated pair hi + lo of floats
+// (about 48 significant bits); converted to double once per thread, and the
+// block and grid sums are FP64.
+struct FFAcc {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float a, float a_lo)
+    {
+        const FF s = two_sum(hi, a);
+        const float e = __fadd_rn(s.lo, __fadd_rn(lo, a_lo));
+        hi = __fadd_rn(s.hi, e);
+        lo = __fsub_rn(e, __fsub_rn(hi, s.hi));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// x^2 as hi + lo: the product and its exact rounding error (one FMA).
+__device__ __forceinline__ void acc_square(FFAcc &acc, float x)
+{
+    const float sq = __fmul_rn(x, x);
+    acc.add(sq, __fmaf_rn(x, x, -sq));
 }
 
 // Divergence, src/fluid.cpp:218-237 (gamma = (float)(-1.0/dt) from the host);
@@ -108,7 +159,7 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ u,
                                                     float *__restrict__ b, int ld, int w, int h, float gamma,
                                                     Reduce red)
 {
-    double acc = 0.0;
+    FFAcc acc;
     for (int j = blockIdx.x; j < h; j += gridDim.x) {
         const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
         for (int i = threadIdx.x; i < w; i += blockDim.x) {
@@ -116,52 +167,65 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ u,
             const float dv = fsub(v[rp + i], v[rm + i]);
             const float bv = fmul(gamma, fadd(du, dv));
             b[r + i] = bv;
-            acc = __fma_rn((double)bv, (double)bv, acc);
+            acc_square(acc, bv);
         }
     }
-    reduce_blocks(acc, red, 1);
+    reduce_blocks(acc.value(), red, 1);
 }
 
-// Residual of the pressure system (src/fluid.cpp:239-257 solves 4p - sum nb = b):
-// r = ((((b + pL) + pR) + pT) + pB) - 4p, evaluated in double.
-__global__ void __launch_bounds__(256) k_residual(const float *__restrict__ p, const float *__restrict__ b, int ld,
-                                                  int w, int h, Reduce red)
+// Residual of the pressure system (src/fluid.cpp:239-257 solves 4p - sum nb = b),
+// r = b + pL + pR + pT + pB - 4p. The five additions are error-free (TwoSum),
+// so hi + lo carries r with a relative error near 2^-48 (the error terms are
+// summed in float). r^2 = hi^2 + (fma error of hi^2) + 2 hi lo is added to
+// the float-float accumulator.
+__device__ __forceinline__ void residual_sq(FFAcc &acc, float b, float l, float r, float t, float bo, float c)
 {
-    double acc = 0.0;
+    FF s = two_sum(b, l);
+    float e = s.lo;
+    s = two_sum(s.hi, r);
+    e = __fadd_rn(e, s.lo);
+    s = two_sum(s.hi, t);
+    e = __fadd_rn(e, s.lo);
+    s = two_sum(s.hi, bo);
+    e = __fadd_rn(e, s.lo);
+    s = two_sum(s.hi, __fmul_rn(-4.0f, c));  // -4p is exact
+    e = __fadd_rn(e, s.lo);
+    const FF q = two_sum(s.hi, e);
+    const float sq = __fmul_rn(q.hi, q.hi);
+    const float sq_err = __fmaf_rn(q.hi, q.hi, -sq);
+    const float cross = __fmul_rn(__fmul_rn(2.0f, q.hi), q.lo);
+    acc.add(sq, __fadd_rn(sq_err, cross));
+}
+
+__global__ void __launch_bounds__(256) k_residual(const float *__restrict__ p, const float *__restrict__ b, int ld,
+                                                  int w, int h, Reduce red, SolveState *state, int sweeps_here,
+                                                  double tol)
+{
+    if (state && *(volatile int *)&state->done) return;  // same answer for every block
+    FFAcc acc;
     for (int j = blockIdx.x; j < h; j += gridDim.x) {
         const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
-        for (int i = threadIdx.x; i < w; i += blockDim.x) {
-            double q = __dadd_rn((double)b[r + i], (double)p[r + wm(i, w)]);
-            q = __dadd_rn(q, (double)p[r + wp(i, w)]);
-            q = __dadd_rn(q, (double)p[rm + i]);
-            q = __dadd_rn(q, (double)p[rp + i]);
-            q = __dsub_rn(q, __dmul_rn(4.0, (double)p[r + i]));
-            acc = __fma_rn(q, q, acc);
-        }
+        for (int i = threadIdx.x; i < w; i += blockDim.x)
+            residual_sq(acc, b[r + i], p[r + wm(i, w)], p[r + wp(i, w)], p[rm + i], p[rp + i], p[r + i]);
     }
-    reduce_blocks(acc, red, 0);
+    reduce_blocks(acc.value(), red, 0, state, sweeps_here, tol);
 }
 
 __global__ void __launch_bounds__(256) k_norms(const float *__restrict__ p, const float *__restrict__ b, int ld, int w,
                                                int h, Reduce red)
 {
-    double acc = 0.0, accb = 0.0;
+    FFAcc acc, accb;
     for (int j = blockIdx.x; j < h; j += gridDim.x) {
         const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
         for (int i = threadIdx.x; i < w; i += blockDim.x) {
-            const double bv = (double)b[r + i];
-            double q = __dadd_rn(bv, (double)p[r + wm(i, w)]);
-            q = __dadd_rn(q, (double)p[r + wp(i, w)]);
-            q = __dadd_rn(q, (double)p[rm + i]);
-            q = __dadd_rn(q, (double)p[rp + i]);
-            q = __dsub_rn(q, __dmul_rn(4.0, (double)p[r + i]));
-            acc = __fma_rn(q, q, acc);
-            accb = __fma_rn(bv, bv, accb);
+            const float bv = b[r + i];
+            residual_sq(acc, bv, p[r + wm(i, w)], p[r + wp(i, w)], p[rm + i], p[rp + i], p[r + i]);
+            acc_square(accb, bv);
         }
     }
-    reduce_blocks(acc, red, 0);
+    reduce_blocks(acc.value(), red, 0);
     __syncthreads();
-    reduce_blocks(accb, red, 1);
+    reduce_blocks(accb.value(), red, 1);
 }
 
 // Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2.
@@ -316,9 +380,9 @@ cudaError_t launch_divergence(const float *u, const float *v, float *b, int ld, 
 }
 
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
-                            cudaStream_t st)
+                            SolveState *state, int sweeps_here, double tol, cudaStream_t st)
 {
-    k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red);
+    k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red, state, sweeps_here, tol);
     return launched();
 }
 

@@ -22,8 +22,9 @@
 namespace pfs {
 
 __global__ void k_sweep_single(const float *__restrict__ pin, const float *__restrict__ b,
-                               float *__restrict__ pout, int ld, int w, int h)
+                               float *__restrict__ pout, int ld, int w, int h, const int *done)
 {
+    if (done && *(volatile const int *)done) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= w || j >= h) return;
@@ -36,26 +37,30 @@ __global__ void k_sweep_single(const float *__restrict__ pin, const float *__res
 
 namespace {
 
-__device__ __forceinline__ int wrap_row(int y, int h)
-{
-    int r = y % h;
-    return r < 0 ? r + h : r;
-}
-
-__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
-
 // Level s+1 of the lane's four cells of row r from level s: `c` is row r
 // (horizontal neighbours from lanes l-1 / l+1), `up` row r-1, `dn` row r+1.
+// Per cell this is ((((l + r) + t) + bo) + b) * 0.25 with one rounding per
+// operation, as pfs::jacobi_p. The first add pairs values from different
+// lanes and runs as four scalar adds; the remaining adds and the scale act on
+// the aligned pairs (x, y) and (z, w) with the packed f32x2 instructions of
+// sm_100+ (__fadd2_rn / __fmul2_rn round each element to nearest, like
+// __fadd_rn), which halves their issue slots.
 __device__ __forceinline__ float4 jacobi4(const float4 &c, const float4 &up, const float4 &dn, const float4 &bb)
 {
     const float lft = __shfl_up_sync(0xffffffffu, c.w, 1);
     const float rgt = __shfl_down_sync(0xffffffffu, c.x, 1);
-    float4 o;
-    o.x = jacobi_p(lft, c.y, up.x, dn.x, bb.x);
-    o.y = jacobi_p(c.x, c.z, up.y, dn.y, bb.y);
-    o.z = jacobi_p(c.y, c.w, up.z, dn.z, bb.z);
-    o.w = jacobi_p(c.z, rgt, up.w, dn.w, bb.w);
-    return o;
+    float2 a = make_float2(__fadd_rn(lft, c.y), __fadd_rn(c.x, c.z));
+    float2 z = make_float2(__fadd_rn(c.y, c.w), __fadd_rn(c.z, rgt));
+    a = __fadd2_rn(a, make_float2(up.x, up.y));
+    z = __fadd2_rn(z, make_float2(up.z, up.w));
+    a = __fadd2_rn(a, make_float2(dn.x, dn.y));
+    z = __fadd2_rn(z, make_float2(dn.z, dn.w));
+    a = __fadd2_rn(a, make_float2(bb.x, bb.y));
+    z = __fadd2_rn(z, make_float2(bb.z, bb.w));
+    const float2 q = make_float2(0.25f, 0.25f);
+    a = __fmul2_rn(a, q);
+    z = __fmul2_rn(z, q);
+    return make_float4(a.x, a.y, z.x, z.y);
 }
 
 struct StreamArgs {
@@ -63,54 +68,105 @@ struct StreamArgs {
     const float *b;
     float *pout;
     float *pprev;  // receives level L-1 (the second-to-last iterate) when non-null
+    const int *done;  // solve already converged: return at once
     int ld, w, h;
     int nsx, nwork, chunk;
 };
 
-// One row step of the pipeline for load row y. P/Cur/N are the three rotating
-// register sets (rows y-s-2, y-s-1, y-s of level s); the caller rotates the
-// roles by passing them in a different order each step, so no register moves
-// are needed.
-template <int L, bool PREV>
-__device__ __forceinline__ void stream_step(int y, float4 (&P)[L], float4 (&Cur)[L], float4 (&N)[L],
-                                            float4 (&bq)[L], float4 &blast, float4 &pn, float4 &bn,
-                                            const StreamArgs &a, int cx, bool st_lane, int y0, int y1, int yend)
+// Rows in flight per warp (cp.async prefetch depth).
+constexpr int kRP = 4;  // power of two
+
+// Per-warp shared-memory rings. p: kRP rows. b: level s+1 of the pipeline
+// reads b of row t-s-1, so the rows t-L .. t+kRP-1 are live: RB = L + kRP
+// rows. Every b row is stored twice (slots k and k + RB), so the L rows a
+// step reads are contiguous from one base slot and each level's address is a
+// compile-time offset from it.
+template <int L>
+struct Ring {
+    static constexpr int RB = L + kRP;
+    static constexpr int floats4_per_warp = (kRP + 2 * RB) * 32;
+    static constexpr int bytes_per_block = 4 * floats4_per_warp * 16;
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
-    N[0] = pn;
-    const float4 b_y = bn;
-    if (y + 1 < yend) {
-        const size_t o = (size_t)wrap_row(y + 1, a.h) * a.ld + cx;
-        pn = ldg4(a.pin + o);
-        bn = ldg4(a.b + o);
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+struct Cursor {
+    const float *gp, *gb;  // next row to prefetch (p and b planes, lane column)
+    int ld_row;            // its row index (wrapped)
+    int wr;                // b ring slot of the next prefetched row
+    long long st_off;      // offset of the level-L row of this step, in floats from the lane column
+    int st_rel;            // that row minus y0 (stored when 0 <= st_rel < rows)
+};
+
+// Issue the cp.async of the next row into p slot `pslot` and b slots wr, wr+RB.
+template <int L>
+__device__ __forceinline__ void prefetch_row(Cursor &cu, float4 *pr, float4 *br, int pslot, const StreamArgs &a)
+{
+    constexpr int RB = Ring<L>::RB;
+    cp_async16(pr + pslot * 32, cu.gp);
+    cp_async16(br + cu.wr * 32, cu.gb);
+    cp_async16(br + (cu.wr + RB) * 32, cu.gb);
+    if (++cu.ld_row == a.h) {
+        cu.ld_row = 0;
+        cu.gp -= (size_t)(a.h - 1) * a.ld;
+        cu.gb -= (size_t)(a.h - 1) * a.ld;
+    } else {
+        cu.gp += a.ld;
+        cu.gb += a.ld;
     }
-#pragma unroll
-    for (int s = L - 1; s > 0; --s) bq[s] = bq[s - 1];
-    bq[0] = blast;  // b(y-1)
-    blast = b_y;
+    cu.wr = (cu.wr + 1 == RB) ? 0 : cu.wr + 1;
+}
+
+// One row step t of the pipeline (load row y = ybeg + t). P/Cur/N are the
+// three rotating register sets (rows y-s-2, y-s-1, y-s of level s); the
+// caller rotates the roles by passing them in a different order each step,
+// so no register moves are needed.
+template <int L, bool PREV>
+__device__ __forceinline__ void stream_step(int t, float4 (&P)[L], float4 (&Cur)[L], float4 (&N)[L], float4 *pr,
+                                            float4 *br, Cursor &cu, const StreamArgs &a, int nsteps, int rows,
+                                            float *out, float *outp)
+{
+    constexpr int RB = Ring<L>::RB;
+    if (t + kRP - 1 < nsteps)
+        prefetch_row<L>(cu, pr, br, (t + kRP - 1) & (kRP - 1), a);
+    else
+        cu.wr = (cu.wr + 1 == RB) ? 0 : cu.wr + 1;  // keep the ring position in step at the tail
+    cp_async_commit();
+    // rows t-L .. t-1 of b start at slot (t - L) mod RB == wr (after this step's prefetch)
+    const float4 *bw = br + cu.wr * 32;
+    cp_async_wait<kRP - 1>();  // row t has landed
+    N[0] = pr[(t & (kRP - 1)) * 32];
     float4 top;
 #pragma unroll
     for (int s = 0; s < L; ++s) {
-        const float4 o = jacobi4(Cur[s], P[s], N[s], bq[s]);  // level s+1, row y-s-1
+        const float4 bb = bw[(L - 1 - s) * 32];               // b of row y-s-1
+        const float4 o = jacobi4(Cur[s], P[s], N[s], bb);     // level s+1, row y-s-1
         if (s + 1 < L) N[s + 1] = o;
         else top = o;
     }
-    const int r = y - L;  // row of level L
-    if (st_lane && r >= y0 && r < y1)
-        *reinterpret_cast<float4 *>(a.pout + (size_t)r * a.ld + cx) = top;
-    if (PREV) {
-        const int rp = y - (L - 1);  // row of level L-1
-        if (st_lane && rp >= y0 && rp < y1)
-            *reinterpret_cast<float4 *>(a.pprev + (size_t)rp * a.ld + cx) = N[L - 1];
-    }
+    if (out && (unsigned)cu.st_rel < (unsigned)rows) *reinterpret_cast<float4 *>(out + cu.st_off) = top;
+    if (PREV && outp && (unsigned)(cu.st_rel + 1) < (unsigned)rows)
+        *reinterpret_cast<float4 *>(outp + cu.st_off + a.ld) = N[L - 1];
+    cu.st_off += a.ld;
+    cu.st_rel += 1;
 }
 
 template <int G, int L, bool PREV>
-__global__ void __launch_bounds__(128) k_sweep_stream(StreamArgs a)
+__global__ void __launch_bounds__(128, 3) k_sweep_stream(StreamArgs a)
 {
     static_assert(L >= 1 && L <= G && G % 4 == 0, "fusion depth must fit the halo");
-    const int lane = threadIdx.x & 31;
-    const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    extern __shared__ float4 sm_rings[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int wid = blockIdx.x * 4 + wib;
     if (wid >= a.nwork) return;  // whole warp
+    if (a.done && *(volatile const int *)a.done) return;
     const int sx = wid % a.nsx, sy = wid / a.nsx;
     const int xo = sx * (128 - 2 * G);
     const int xl = xo - G + 4 * lane;
@@ -118,29 +174,57 @@ __global__ void __launch_bounds__(128) k_sweep_stream(StreamArgs a)
     if (cx < 0) cx += a.w;
     const bool st_lane = lane >= G / 4 && lane < 32 - G / 4 && xl < a.w;
     const int y0 = sy * a.chunk;
-    const int y1 = min(a.h, y0 + a.chunk);
-    const int ybeg = y0 - L, yend = y1 + L;
+    const int rows = min(a.h, y0 + a.chunk) - y0;
+    const int ybeg = y0 - L;
+    const int nsteps = rows + 2 * L;
 
-    float4 R0[L], R1[L], R2[L], bq[L];
+    float4 *pr = sm_rings + wib * Ring<L>::floats4_per_warp + lane;
+    float4 *br = pr + kRP * 32;
+
+    Cursor cu;
+    cu.ld_row = ybeg % a.h;
+    if (cu.ld_row < 0) cu.ld_row += a.h;
+    cu.gp = a.pin + (size_t)cu.ld_row * a.ld + cx;
+    cu.gb = a.b + (size_t)cu.ld_row * a.ld + cx;
+    cu.wr = 0;
+    cu.st_rel = -2 * L;  // level L at step 0 is row ybeg - L = y0 - 2L
+    cu.st_off = (long long)(y0 - 2 * L) * a.ld;
+    float *out = st_lane ? a.pout + cx : nullptr;
+    float *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
+#pragma unroll
+    for (int k = 0; k < kRP - 1; ++k) {
+        if (k < nsteps) prefetch_row<L>(cu, pr, br, k, a);
+        cp_async_commit();
+    }
+    // after the prologue wr = (kRP - 1) mod RB; step t advances it before reading,
+    // so at step t it equals (t + kRP) mod RB == (t - L) mod RB.
+
+    float4 R0[L], R1[L], R2[L];
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int s = 0; s < L; ++s) R0[s] = R1[s] = R2[s] = bq[s] = z;
-    float4 blast = z;
-    const size_t o0 = (size_t)wrap_row(ybeg, a.h) * a.ld + cx;
-    float4 pn = ldg4(a.pin + o0), bn = ldg4(a.b + o0);
+    for (int s = 0; s < L; ++s) R0[s] = R1[s] = R2[s] = z;
 
-    for (int y = ybeg; y < yend; y += 3) {
-        stream_step<L, PREV>(y, R0, R1, R2, bq, blast, pn, bn, a, cx, st_lane, y0, y1, yend);
-        if (y + 1 < yend) stream_step<L, PREV>(y + 1, R1, R2, R0, bq, blast, pn, bn, a, cx, st_lane, y0, y1, yend);
-        if (y + 2 < yend) stream_step<L, PREV>(y + 2, R2, R0, R1, bq, blast, pn, bn, a, cx, st_lane, y0, y1, yend);
+    for (int t = 0; t < nsteps; t += 3) {
+        stream_step<L, PREV>(t, R0, R1, R2, pr, br, cu, a, nsteps, rows, out, outp);
+        if (t + 1 < nsteps) stream_step<L, PREV>(t + 1, R1, R2, R0, pr, br, cu, a, nsteps, rows, out, outp);
+        if (t + 2 < nsteps) stream_step<L, PREV>(t + 2, R2, R0, R1, pr, br, cu, a, nsteps, rows, out, outp);
     }
+    cp_async_wait<0>();
 }
 
 template <int G, int L, bool PREV>
 cudaError_t launch_stream_t(const StreamArgs &a, cudaStream_t st)
 {
-    const int blocks = (a.nwork + 3) / 4;
-    k_sweep_stream<G, L, PREV><<<blocks, 128, 0, st>>>(a);
+    constexpr int smem = Ring<L>::bytes_per_block;
+    static bool attr_set = false;  // per instantiation; the attribute is per function
+    if (!attr_set) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_sweep_stream<G, L, PREV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const int blocks = (a.nwork + 3) / 4;  // 4 warps per block: the shared rings are laid out for 4
+    k_sweep_stream<G, L, PREV><<<blocks, 128, smem, st>>>(a);
     return launched();
 }
 
@@ -155,19 +239,20 @@ cudaError_t launch_stream_l(const StreamArgs &a, bool prev, cudaStream_t st)
 int stream_strip_width(int halo) { return 128 - 2 * halo; }
 
 cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, int ld, int w, int h,
-                                cudaStream_t st)
+                                const int *done, cudaStream_t st)
 {
     dim3 blk(32, 8);
     dim3 grd((w + 31) / 32, (h + 7) / 8);
-    k_sweep_single<<<grd, blk, 0, st>>>(pin, b, pout, ld, w, h);
+    k_sweep_single<<<grd, blk, 0, st>>>(pin, b, pout, ld, w, h, done);
     return launched();
 }
 
 // levels in [1, halo]; halo in {4, 8}; w % 4 == 0; ld % 4 == 0; 16-byte aligned planes.
 cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
-                                int h, int levels, int halo, int chunk, cudaStream_t st)
+                                int h, int levels, int halo, int chunk, const int *done, cudaStream_t st)
 {
     StreamArgs a;
+    a.done = done;
     a.pin = pin;
     a.b = b;
     a.pout = pout;
