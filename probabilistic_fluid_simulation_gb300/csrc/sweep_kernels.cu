@@ -76,15 +76,19 @@ struct StreamArgs {
 // Rows in flight per warp (cp.async prefetch depth).
 constexpr int kRP = 4;  // power of two
 
-// Per-warp shared-memory rings. p: kRP rows. b: level s+1 of the pipeline
-// reads b of row t-s-1, so the rows t-L .. t+kRP-1 are live: RB = L + kRP
-// rows. Every b row is stored twice (slots k and k + RB), so the L rows a
-// step reads are contiguous from one base slot and each level's address is a
-// compile-time offset from it.
+constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
+
+// Register rings of the pipeline. Level s (0..L-1) keeps rows y-s-2, y-s-1,
+// y-s in three register sets whose roles rotate with period 3; the divergence
+// rows y-1 .. y-L plus the row being loaded live in a ring of L+1 registers.
+// Unrolling the row loop by U = lcm(3, L+1) makes every ring index a
+// compile-time register name: no register moves, one shared-memory read of b
+// per row instead of one per level.
 template <int L>
 struct Ring {
-    static constexpr int RB = L + kRP;
-    static constexpr int floats4_per_warp = (kRP + 2 * RB) * 32;
+    static constexpr int NB = L + 1;
+    static constexpr int U = 3 * NB / gcd_c(3, NB);
+    static constexpr int floats4_per_warp = 2 * kRP * 32;  // p and b prefetch rings
     static constexpr int bytes_per_block = 4 * floats4_per_warp * 16;
 };
 
@@ -100,19 +104,15 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 struct Cursor {
     const float *gp, *gb;  // next row to prefetch (p and b planes, lane column)
     int ld_row;            // its row index (wrapped)
-    int wr;                // b ring slot of the next prefetched row
     long long st_off;      // offset of the level-L row of this step, in floats from the lane column
     int st_rel;            // that row minus y0 (stored when 0 <= st_rel < rows)
 };
 
-// Issue the cp.async of the next row into p slot `pslot` and b slots wr, wr+RB.
-template <int L>
-__device__ __forceinline__ void prefetch_row(Cursor &cu, float4 *pr, float4 *br, int pslot, const StreamArgs &a)
+// Issue the cp.async of the next row into ring slot `slot` of p and b.
+__device__ __forceinline__ void prefetch_row(Cursor &cu, float4 *pr, float4 *br, int slot, const StreamArgs &a)
 {
-    constexpr int RB = Ring<L>::RB;
-    cp_async16(pr + pslot * 32, cu.gp);
-    cp_async16(br + cu.wr * 32, cu.gb);
-    cp_async16(br + (cu.wr + RB) * 32, cu.gb);
+    cp_async16(pr + slot * 32, cu.gp);
+    cp_async16(br + slot * 32, cu.gb);
     if (++cu.ld_row == a.h) {
         cu.ld_row = 0;
         cu.gp -= (size_t)(a.h - 1) * a.ld;
@@ -121,33 +121,29 @@ __device__ __forceinline__ void prefetch_row(Cursor &cu, float4 *pr, float4 *br,
         cu.gp += a.ld;
         cu.gb += a.ld;
     }
-    cu.wr = (cu.wr + 1 == RB) ? 0 : cu.wr + 1;
 }
 
-// One row step t of the pipeline (load row y = ybeg + t). P/Cur/N are the
-// three rotating register sets (rows y-s-2, y-s-1, y-s of level s); the
-// caller rotates the roles by passing them in a different order each step,
-// so no register moves are needed.
-template <int L, bool PREV>
-__device__ __forceinline__ void stream_step(int t, float4 (&P)[L], float4 (&Cur)[L], float4 (&N)[L], float4 *pr,
-                                            float4 *br, Cursor &cu, const StreamArgs &a, int nsteps, int rows,
-                                            float *out, float *outp)
+// One row step t of the pipeline (load row y = ybeg + t); K = t mod U is a
+// compile-time constant, so R[K % 3]... and bq[...] name fixed registers.
+template <int L, bool PREV, int K>
+__device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[L + 1], float4 *pr, float4 *br,
+                                            Cursor &cu, const StreamArgs &a, int nsteps, int rows, float *out,
+                                            float *outp)
 {
-    constexpr int RB = Ring<L>::RB;
-    if (t + kRP - 1 < nsteps)
-        prefetch_row<L>(cu, pr, br, (t + kRP - 1) & (kRP - 1), a);
-    else
-        cu.wr = (cu.wr + 1 == RB) ? 0 : cu.wr + 1;  // keep the ring position in step at the tail
+    constexpr int NB = L + 1;
+    float4(&P)[L] = R[K % 3];
+    float4(&Cur)[L] = R[(K + 1) % 3];
+    float4(&N)[L] = R[(K + 2) % 3];
+    if (t + kRP - 1 < nsteps) prefetch_row(cu, pr, br, (t + kRP - 1) & (kRP - 1), a);
     cp_async_commit();
-    // rows t-L .. t-1 of b start at slot (t - L) mod RB == wr (after this step's prefetch)
-    const float4 *bw = br + cu.wr * 32;
     cp_async_wait<kRP - 1>();  // row t has landed
     N[0] = pr[(t & (kRP - 1)) * 32];
+    bq[K % NB] = br[(t & (kRP - 1)) * 32];  // b of row y, first used at the next step
     float4 top;
 #pragma unroll
     for (int s = 0; s < L; ++s) {
-        const float4 bb = bw[(L - 1 - s) * 32];               // b of row y-s-1
-        const float4 o = jacobi4(Cur[s], P[s], N[s], bb);     // level s+1, row y-s-1
+        const float4 &bb = bq[(K + NB * L - s - 1) % NB];  // b of row y-s-1
+        const float4 o = jacobi4(Cur[s], P[s], N[s], bb);   // level s+1, row y-s-1
         if (s + 1 < L) N[s + 1] = o;
         else top = o;
     }
@@ -158,8 +154,26 @@ __device__ __forceinline__ void stream_step(int t, float4 (&P)[L], float4 (&Cur)
     cu.st_rel += 1;
 }
 
+template <int L, bool PREV, int K>
+__device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[L + 1], float4 *pr, float4 *br,
+                                             Cursor &cu, const StreamArgs &a, int nsteps, int rows, float *out,
+                                             float *outp)
+{
+    if constexpr (K < Ring<L>::U) {
+        if (t + K < nsteps) {
+            stream_step<L, PREV, K>(t + K, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_steps<L, PREV, K + 1>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+        }
+    }
+}
+
+// Blocks per SM the register budget aims for: the deepest pipelines need
+// more than 65536 / (3 * 128) registers per thread without spilling.
+template <int L>
+constexpr int min_blocks() { return L >= 7 ? 2 : 3; }
+
 template <int G, int L, bool PREV>
-__global__ void __launch_bounds__(128, 3) k_sweep_stream(StreamArgs a)
+__global__ void __launch_bounds__(128, min_blocks<L>()) k_sweep_stream(StreamArgs a)
 {
     static_assert(L >= 1 && L <= G && G % 4 == 0, "fusion depth must fit the halo");
     extern __shared__ float4 sm_rings[];
@@ -186,29 +200,25 @@ __global__ void __launch_bounds__(128, 3) k_sweep_stream(StreamArgs a)
     if (cu.ld_row < 0) cu.ld_row += a.h;
     cu.gp = a.pin + (size_t)cu.ld_row * a.ld + cx;
     cu.gb = a.b + (size_t)cu.ld_row * a.ld + cx;
-    cu.wr = 0;
     cu.st_rel = -2 * L;  // level L at step 0 is row ybeg - L = y0 - 2L
     cu.st_off = (long long)(y0 - 2 * L) * a.ld;
     float *out = st_lane ? a.pout + cx : nullptr;
     float *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
 #pragma unroll
     for (int k = 0; k < kRP - 1; ++k) {
-        if (k < nsteps) prefetch_row<L>(cu, pr, br, k, a);
+        if (k < nsteps) prefetch_row(cu, pr, br, k, a);
         cp_async_commit();
     }
-    // after the prologue wr = (kRP - 1) mod RB; step t advances it before reading,
-    // so at step t it equals (t + kRP) mod RB == (t - L) mod RB.
 
-    float4 R0[L], R1[L], R2[L];
+    float4 R[3][L], bq[L + 1];
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int s = 0; s < L; ++s) R0[s] = R1[s] = R2[s] = z;
+    for (int s = 0; s < L; ++s) R[0][s] = R[1][s] = R[2][s] = z;
+#pragma unroll
+    for (int s = 0; s <= L; ++s) bq[s] = z;
 
-    for (int t = 0; t < nsteps; t += 3) {
-        stream_step<L, PREV>(t, R0, R1, R2, pr, br, cu, a, nsteps, rows, out, outp);
-        if (t + 1 < nsteps) stream_step<L, PREV>(t + 1, R1, R2, R0, pr, br, cu, a, nsteps, rows, out, outp);
-        if (t + 2 < nsteps) stream_step<L, PREV>(t + 2, R2, R0, R1, pr, br, cu, a, nsteps, rows, out, outp);
-    }
+    for (int t = 0; t < nsteps; t += Ring<L>::U)
+        stream_steps<L, PREV, 0>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
     cp_async_wait<0>();
 }
 

@@ -1,0 +1,87 @@
+"""Timing and tuning of the fused pressure sweep (k_sweep_stream).
+
+    python -m probabilistic_fluid_simulation_gb300.tune --size 2048 --levels 8 --chunk 32
+    python -m probabilistic_fluid_simulation_gb300.tune --size 2048 --scan
+
+Times back-to-back launches of `levels` fused sweeps on random planar
+fields with CUDA events on the launching stream and prints microseconds per
+launch and cell-sweeps per second. --scan times every (levels, chunk rows)
+candidate and prints the fastest; `best_config` is the same search as a
+function (used to pick a session's fuse depth and chunk height).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import fluid
+
+LEVELS = (4, 8)
+CHUNKS = (16, 24, 32, 48, 64, 96)
+
+
+def time_sweeps(size: int, levels: int, chunk: int, reps: int = 100, warm: int = 5, height: int = 0) -> float:
+    """Microseconds per fused launch of `levels` sweeps on a size x height grid."""
+    import torch
+    h = height or size
+    ld = (size + 31) // 32 * 32
+    g = torch.Generator(device="cpu").manual_seed(0)
+    p = torch.randn(h, ld, generator=g).cuda()
+    b = torch.randn(h, ld, generator=g).cuda()
+    q = torch.empty_like(p)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def run(n):
+        for i in range(n):
+            src, dst = (p, q) if i % 2 == 0 else (q, p)
+            fluid.pressure_sweeps(src, b, dst, None, levels, fused=True, chunk_rows=chunk, w=size, stream=stream)
+
+    run(warm)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run(reps)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) * 1e3 / reps
+
+
+def best_config(size: int, height: int = 0, levels=LEVELS, chunks=CHUNKS, reps: int = 50):
+    """(levels, chunk, us_per_sweep) with the lowest time per sweep."""
+    best = None
+    for lv in levels:
+        for ch in chunks:
+            us = time_sweeps(size, lv, ch, reps=reps, height=height) / lv
+            if best is None or us < best[2]:
+                best = (lv, ch, us)
+    return best
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--height", type=int, default=0)
+    ap.add_argument("--levels", type=int, default=8)
+    ap.add_argument("--chunk", type=int, default=32)
+    ap.add_argument("--reps", type=int, default=100)
+    ap.add_argument("--scan", action="store_true")
+    a = ap.parse_args()
+    cells = a.size * (a.height or a.size)
+    if a.scan:
+        rows = []
+        for lv in LEVELS:
+            for ch in CHUNKS:
+                us = time_sweeps(a.size, lv, ch, reps=a.reps, height=a.height)
+                rows.append({"levels": lv, "chunk": ch, "us_per_launch": us,
+                             "cell_sweeps_per_s": cells * lv / (us * 1e-6)})
+                print(json.dumps(rows[-1]), flush=True)
+        best = max(rows, key=lambda r: r["cell_sweeps_per_s"])
+        print(json.dumps({"best": best}))
+    else:
+        us = time_sweeps(a.size, a.levels, a.chunk, reps=a.reps, height=a.height)
+        print(json.dumps({"size": a.size, "levels": a.levels, "chunk": a.chunk, "us_per_launch": us,
+                          "cell_sweeps_per_s": cells * a.levels / (us * 1e-6)}))
+
+
+if __name__ == "__main__":
+    main()
