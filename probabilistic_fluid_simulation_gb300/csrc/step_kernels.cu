@@ -2,6 +2,8 @@
 // layout conversion and the residual reduction, on planar float32 fields.
 // Each kernel follows one routine of the reference's src/fluid.cpp (cited
 // per kernel) with the same per-cell arithmetic, so results are bit-equal.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -228,6 +230,62 @@ __global__ void __launch_bounds__(256) k_norms(const float *__restrict__ p, cons
     reduce_blocks(accb.value(), red, 1);
 }
 
+// Residual on warp strips (w % 4 == 0): each warp covers 128 columns (four
+// per lane, float4 rows) and a chunk of rows, keeping rows r-1, r, r+1 of p in
+// registers; left/right neighbours come from the adjacent lanes by shuffle,
+// and the lanes at the strip edges read their outside neighbour directly.
+// Same per-cell arithmetic as residual_sq, so the same sums.
+constexpr int kResChunk = 32;
+
+__global__ void __launch_bounds__(128) k_residual_strip(const float *__restrict__ p, const float *__restrict__ b,
+                                                        int ld, int w, int h, int nsx, int nwork, Reduce red,
+                                                        SolveState *state, int sweeps_here, double tol, int with_b)
+{
+    if (state && *(volatile int *)&state->done) return;  // same answer for every block
+    const int lane = threadIdx.x & 31;
+    FFAcc acc, accb;
+    for (int wid = blockIdx.x * 4 + (threadIdx.x >> 5); wid < nwork; wid += gridDim.x * 4) {
+        const int sx = wid % nsx, sy = wid / nsx;
+        const int x = sx * 128 + 4 * lane;
+        const bool active = x < w;
+        const int xs = active ? x : w - 4;  // inactive lanes shadow a valid column, results discarded
+        const int last_lane = min(31, (w - sx * 128) / 4 - 1);
+        const int xl = (sx * 128 == 0) ? w - 1 : sx * 128 - 1;         // left outside neighbour
+        const int xr = (sx * 128 + 4 * (last_lane + 1)) % w;           // right outside neighbour
+        const int y0 = sy * kResChunk, y1 = min(h, y0 + kResChunk);
+        const float *pc = p + xs;
+        float4 up = *reinterpret_cast<const float4 *>(pc + (size_t)wm(y0, h) * ld);
+        float4 cu = *reinterpret_cast<const float4 *>(pc + (size_t)y0 * ld);
+        for (int y = y0; y < y1; ++y) {
+            const float4 dn = *reinterpret_cast<const float4 *>(pc + (size_t)wp(y, h) * ld);
+            const float4 bb = *reinterpret_cast<const float4 *>(b + (size_t)y * ld + xs);
+            float lft = __shfl_up_sync(0xffffffffu, cu.w, 1);
+            float rgt = __shfl_down_sync(0xffffffffu, cu.x, 1);
+            if (lane == 0) lft = p[(size_t)y * ld + xl];
+            if (lane == last_lane) rgt = p[(size_t)y * ld + xr];
+            if (active) {
+                residual_sq(acc, bb.x, lft, cu.y, up.x, dn.x, cu.x);
+                residual_sq(acc, bb.y, cu.x, cu.z, up.y, dn.y, cu.y);
+                residual_sq(acc, bb.z, cu.y, cu.w, up.z, dn.z, cu.z);
+                residual_sq(acc, bb.w, cu.z, rgt, up.w, dn.w, cu.w);
+                if (with_b) {
+                    acc_square(accb, bb.x);
+                    acc_square(accb, bb.y);
+                    acc_square(accb, bb.z);
+                    acc_square(accb, bb.w);
+                }
+            }
+            up = cu;
+            cu = dn;
+        }
+    }
+    reduce_blocks(acc.value(), red, 0, state, sweeps_here, tol);
+    if (with_b) {
+        __syncthreads();
+        reduce_blocks(accb.value(), red, 1);
+    }
+}
+
 // Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2.
 __device__ __forceinline__ void project_cell(const float *__restrict__ u, const float *__restrict__ v,
                                              const float *__restrict__ p, int ld, int w, int h, float dt, int i,
@@ -379,15 +437,36 @@ cudaError_t launch_divergence(const float *u, const float *v, float *b, int ld, 
     return launched();
 }
 
+static bool strip_ok(int w, int ld) { return w % 4 == 0 && ld % 4 == 0; }
+
+static void strip_grid(int w, int h, int nblocks_max, int &nsx, int &nwork, int &blocks)
+{
+    nsx = (w + 127) / 128;
+    nwork = nsx * ((h + kResChunk - 1) / kResChunk);
+    blocks = std::min((nwork + 3) / 4, nblocks_max);
+}
+
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
                             SolveState *state, int sweeps_here, double tol, cudaStream_t st)
 {
+    if (strip_ok(w, ld)) {
+        int nsx, nwork, blocks;
+        strip_grid(w, h, red.nblocks, nsx, nwork, blocks);
+        k_residual_strip<<<blocks, 128, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, state, sweeps_here, tol, 0);
+        return launched();
+    }
     k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red, state, sweeps_here, tol);
     return launched();
 }
 
 cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, const Reduce &red, cudaStream_t st)
 {
+    if (strip_ok(w, ld)) {
+        int nsx, nwork, blocks;
+        strip_grid(w, h, red.nblocks, nsx, nwork, blocks);
+        k_residual_strip<<<blocks, 128, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, nullptr, 0, 0.0, 1);
+        return launched();
+    }
     k_norms<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red);
     return launched();
 }
