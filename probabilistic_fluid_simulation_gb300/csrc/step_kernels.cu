@@ -235,16 +235,19 @@ __global__ void __launch_bounds__(256) k_norms(const float *__restrict__ p, cons
 // registers; left/right neighbours come from the adjacent lanes by shuffle,
 // and the lanes at the strip edges read their outside neighbour directly.
 // Same per-cell arithmetic as residual_sq, so the same sums.
-constexpr int kResChunk = 32;
+constexpr int kResChunk = 8;    // rows per warp
+constexpr int kResWarps = 8;    // warps per block
 
-__global__ void __launch_bounds__(128) k_residual_strip(const float *__restrict__ p, const float *__restrict__ b,
-                                                        int ld, int w, int h, int nsx, int nwork, Reduce red,
-                                                        SolveState *state, int sweeps_here, double tol, int with_b)
+__global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *__restrict__ p,
+                                                                   const float *__restrict__ b, int ld, int w,
+                                                                   int h, int nsx, int nwork, Reduce red,
+                                                                   SolveState *state, int sweeps_here, double tol,
+                                                                   int with_b)
 {
     if (state && *(volatile int *)&state->done) return;  // same answer for every block
     const int lane = threadIdx.x & 31;
-    FFAcc acc, accb;
-    for (int wid = blockIdx.x * 4 + (threadIdx.x >> 5); wid < nwork; wid += gridDim.x * 4) {
+    FFAcc acc[4], accb;  // one accumulator per lane column: four independent chains
+    for (int wid = blockIdx.x * kResWarps + (threadIdx.x >> 5); wid < nwork; wid += gridDim.x * kResWarps) {
         const int sx = wid % nsx, sy = wid / nsx;
         const int x = sx * 128 + 4 * lane;
         const bool active = x < w;
@@ -264,10 +267,10 @@ __global__ void __launch_bounds__(128) k_residual_strip(const float *__restrict_
             if (lane == 0) lft = p[(size_t)y * ld + xl];
             if (lane == last_lane) rgt = p[(size_t)y * ld + xr];
             if (active) {
-                residual_sq(acc, bb.x, lft, cu.y, up.x, dn.x, cu.x);
-                residual_sq(acc, bb.y, cu.x, cu.z, up.y, dn.y, cu.y);
-                residual_sq(acc, bb.z, cu.y, cu.w, up.z, dn.z, cu.z);
-                residual_sq(acc, bb.w, cu.z, rgt, up.w, dn.w, cu.w);
+                residual_sq(acc[0], bb.x, lft, cu.y, up.x, dn.x, cu.x);
+                residual_sq(acc[1], bb.y, cu.x, cu.z, up.y, dn.y, cu.y);
+                residual_sq(acc[2], bb.z, cu.y, cu.w, up.z, dn.z, cu.z);
+                residual_sq(acc[3], bb.w, cu.z, rgt, up.w, dn.w, cu.w);
                 if (with_b) {
                     acc_square(accb, bb.x);
                     acc_square(accb, bb.y);
@@ -279,7 +282,8 @@ __global__ void __launch_bounds__(128) k_residual_strip(const float *__restrict_
             cu = dn;
         }
     }
-    reduce_blocks(acc.value(), red, 0, state, sweeps_here, tol);
+    reduce_blocks((acc[0].value() + acc[1].value()) + (acc[2].value() + acc[3].value()), red, 0, state, sweeps_here,
+                  tol);
     if (with_b) {
         __syncthreads();
         reduce_blocks(accb.value(), red, 1);
@@ -443,7 +447,7 @@ static void strip_grid(int w, int h, int nblocks_max, int &nsx, int &nwork, int 
 {
     nsx = (w + 127) / 128;
     nwork = nsx * ((h + kResChunk - 1) / kResChunk);
-    blocks = std::min((nwork + 3) / 4, nblocks_max);
+    blocks = std::min((nwork + kResWarps - 1) / kResWarps, nblocks_max);
 }
 
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
@@ -452,7 +456,7 @@ cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h
     if (strip_ok(w, ld)) {
         int nsx, nwork, blocks;
         strip_grid(w, h, red.nblocks, nsx, nwork, blocks);
-        k_residual_strip<<<blocks, 128, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, state, sweeps_here, tol, 0);
+        k_residual_strip<<<blocks, kResWarps * 32, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, state, sweeps_here, tol, 0);
         return launched();
     }
     k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red, state, sweeps_here, tol);
@@ -464,7 +468,7 @@ cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, c
     if (strip_ok(w, ld)) {
         int nsx, nwork, blocks;
         strip_grid(w, h, red.nblocks, nsx, nwork, blocks);
-        k_residual_strip<<<blocks, 128, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, nullptr, 0, 0.0, 1);
+        k_residual_strip<<<blocks, kResWarps * 32, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, nullptr, 0, 0.0, 1);
         return launched();
     }
     k_norms<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red);
