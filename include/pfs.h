@@ -187,6 +187,29 @@ int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *
 int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, double *rr, double *bb,
                        void *stream);
 
+/*
+ * pfs_residual_norms without any device allocation. No counterpart in the
+ * reference (whose step allocates nothing and reports no residual); it exists
+ * for callers that must not allocate device memory: a host application whose
+ * device memory is entirely reserved by another allocator (a framework's
+ * caching pool that owns the device) would get out-of-memory from cudaMalloc,
+ * and a caller on a latency-critical path cannot afford cudaMalloc, which may
+ * synchronize the device. pfs_residual_norms allocates its scratch on first use
+ * per device and grid size; this call allocates nothing.
+ *
+ * Same kernel and same results as pfs_residual_norms. Its cross-block scratch
+ * is a fixed 10 KiB array inside the library, present on every device that
+ * loads the library until the process exits. The first call on a device looks
+ * up that array's device address (once per device, with the device current):
+ * make that first call before any stream capture. Every call shares the array
+ * and clears the part that must start at zero itself; calls that overlap on
+ * the GPU (different streams running at the same time) race on it, so issue
+ * them one after another. Grids above 2^30 cells are rejected with
+ * PFS_ERR_INVALID_ARGUMENT. Blocking, like pfs_residual_norms.
+ */
+int pfs_residual_norms_static(const float *p, const float *b, int vx, int vy, int ld, double *rr, double *bb,
+                              void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,16 @@ int fail(int code, const char *fmt, ...)
     return code;
 }
 
+}  // namespace
+
+int pfs::record_error(int code, const char *msg)
+{
+    g_err = msg;
+    return code;
+}
+
+namespace {
+
 #define CK(x)                                                                                              \
     do {                                                                                                   \
         cudaError_t e_ = (x);                                                                              \

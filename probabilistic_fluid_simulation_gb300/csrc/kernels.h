@@ -9,6 +9,9 @@
 
 namespace pfs {
 
+// Record `msg` as the calling thread's pfs_last_error() and return `code`.
+int record_error(int code, const char *msg);
+
 // Kernels launched by this library since it was loaded (pfs_kernel_launches()).
 extern std::atomic<long long> g_launches;
 inline cudaError_t launched(int n = 1)

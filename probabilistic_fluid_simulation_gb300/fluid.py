@@ -92,6 +92,8 @@ SIGNATURES = [
                                       C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("pfs_residual_norms", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.c_void_p]),
+    ("pfs_residual_norms_static", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
 ]
 
 
@@ -277,4 +279,15 @@ def residual_norms(p, b, w: Optional[int] = None, stream: int = 0) -> Tuple[floa
     rr, bb = C.c_double(), C.c_double()
     _check(lib().pfs_residual_norms(C.c_void_p(_ptr(p)), C.c_void_p(_ptr(b)), w or ld, h, ld, C.byref(rr),
                                     C.byref(bb), C.c_void_p(stream or None)))
+    return rr.value, bb.value
+
+
+def residual_norms_static(p, b, w: Optional[int] = None, stream: int = 0) -> Tuple[float, float]:
+    """residual_norms for callers that must not allocate device memory: the
+    reduction's scratch is a fixed array inside the library
+    (pfs_residual_norms_static in include/pfs.h)."""
+    h, ld = p.shape
+    rr, bb = C.c_double(), C.c_double()
+    _check(lib().pfs_residual_norms_static(C.c_void_p(_ptr(p)), C.c_void_p(_ptr(b)), w or ld, h, ld, C.byref(rr),
+                                           C.byref(bb), C.c_void_p(stream or None)))
     return rr.value, bb.value
