@@ -130,6 +130,23 @@ int pfs_advect_color_step_host(pfs_vp_field *image, pfs_vp_field *itmp, pfs_vp_f
  */
 enum { PFS_HOST = 0, PFS_DEVICE = 1 };
 
+/* Storage / arithmetic form of a session:
+ *   PFS_PREC_F32   the reference's float32 arithmetic, bit-exact (default);
+ *   PFS_PREC_BF16  velocity, image and the pressure correction stored bf16,
+ *                  computed in FP32; pressure, residual and the refinement
+ *                  update x += e in FP64 (iterative refinement: the same
+ *                  Jacobi iteration, different rounding);
+ *   PFS_PREC_F16   the same with fp16 storage (the right-hand side of each
+ *                  correction solve is scaled by 1/max|r| into fp16 range);
+ *   PFS_PREC_F64   every field and operation in FP64: the FP64 run of the
+ *                  same method, the yardstick for the others' error.
+ * The non-F32 forms run with viscosity 0 and an even diffusion count (the
+ * reference's buffer roles then reduce to: pressure iteration from the
+ * previous final pressure, projection with the final pressure); other
+ * settings return PFS_ERR_UNSUPPORTED. check_every sets the sweeps between
+ * refinements of the 16-bit forms (0 means 32). */
+enum { PFS_PREC_F32 = 0, PFS_PREC_BF16 = 1, PFS_PREC_F16 = 2, PFS_PREC_F64 = 3 };
+
 typedef struct {
     float dt;
     float viscosity;
@@ -140,6 +157,7 @@ typedef struct {
     int fuse_depth;     /* sweeps fused per launch, 0 = tuned default              */
     int chunk_rows;     /* rows per warp in the fused sweep, 0 = tuned default      */
     int want_residual;  /* fixed mode: also report the final residual              */
+    int precision;      /* PFS_PREC_*                                              */
 } pfs_params;
 
 typedef struct {
@@ -169,6 +187,9 @@ int pfs_session_step(pfs_session *s, int n);
 /* Write the state back in the reference layout (the buffers the reference's
  * vp, tmp and image pointers would designate after the same steps). */
 int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, int where);
+/* The state in float64, interleaved: vp (u, v, pressure, divergence) and the
+ * image. For the F32 form the pressure is the final iterate (tmp's channel 2). */
+int pfs_session_download_f64(pfs_session *s, double *vp, double *image, int where);
 int pfs_session_stats(pfs_session *s, pfs_stats *out);
 int pfs_session_sync(pfs_session *s);
 int pfs_session_destroy(pfs_session *s);

@@ -23,6 +23,7 @@
 
 #include "kernels.h"
 #include "pfs.h"
+#include "precision.h"
 
 using pfs::Reduce;
 
@@ -417,10 +418,12 @@ struct pfs_session {
     size_t stage_bytes = 0;
     pfs_params prm{};
     pfs_stats stats{};
+    pfs::LpState *lp = nullptr;  // precision forms other than F32
     ~pfs_session()
     {
         if (img_mem) cudaFree(img_mem);
         if (stage) cudaFree(stage);
+        if (lp) pfs::lp_destroy(lp);
     }
 };
 
@@ -600,6 +603,14 @@ static int check_params(const pfs_params *p)
     if (p->fuse_depth < 0 || p->fuse_depth > 8) return fail(PFS_ERR_INVALID_ARGUMENT, "fuse_depth in [0, 8]");
     if (p->chunk_rows < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "chunk_rows must be >= 0");
     if (std::isnan(p->tol)) return fail(PFS_ERR_NOT_FINITE, "tol is NaN");
+    if (p->precision < PFS_PREC_F32 || p->precision > PFS_PREC_F64)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "unknown precision form %d", p->precision);
+    if (p->precision != PFS_PREC_F32) {
+        if (p->viscosity != 0.0f)
+            return fail(PFS_ERR_UNSUPPORTED, "precision forms other than F32 run with viscosity 0");
+        if (p->diffuse_iters < 2 || p->diffuse_iters % 2)
+            return fail(PFS_ERR_UNSUPPORTED, "precision forms other than F32 need an even diffusion count >= 2");
+    }
     return PFS_OK;
 }
 
@@ -636,6 +647,25 @@ int pfs_session_create(pfs_session **out, int vx, int vy, int ix, int iy, int iz
     if (!s) return fail(PFS_ERR_CUDA, "out of host memory");
     s->prm = *p;
     s->st = (cudaStream_t)stream;
+    if ((p->precision == PFS_PREC_BF16 || p->precision == PFS_PREC_F16) && vx % 4 != 0) {
+        delete s;
+        return fail(PFS_ERR_UNSUPPORTED, "16-bit forms need a grid width divisible by 4");
+    }
+    if (p->precision != PFS_PREC_F32) {
+        int rc = pfs::lp_create(&s->lp, p->precision, vx, vy, iz > 0 ? ix : 0, iz > 0 ? iy : 0, iz);
+        if (rc == PFS_OK) CK(cudaGetDevice(&s->dev));
+        if (rc != PFS_OK) {
+            delete s;
+            return rc;
+        }
+        s->f.w = vx;  // dims only; the planar F32 fields are not allocated for these forms
+        s->f.h = vy;
+        s->iw = ix;
+        s->ih = iy;
+        s->ic = iz;
+        *out = s;
+        return PFS_OK;
+    }
     int rc = s->f.alloc(vx, vy);
     if (rc == PFS_OK) CK(cudaGetDevice(&s->dev));
     if (rc == PFS_OK && iz > 0) {
@@ -662,6 +692,8 @@ int pfs_session_set_params(pfs_session *s, const pfs_params *params)
 {
     if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
     CKS(check_params(params));
+    if (params->precision != s->prm.precision)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "the precision form is fixed at session creation");
     s->prm = *params;
     return PFS_OK;
 }
@@ -699,6 +731,11 @@ int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const 
         CKS(check_aligned(vp, "vp"));
         CKS(check_aligned(tmp, "tmp"));
     }
+    if (s->lp) {
+        CKS(pfs::lp_upload(s->lp, A, B, I, s->st));
+        if (where == PFS_HOST) CK(cudaStreamSynchronize(s->st));
+        return PFS_OK;
+    }
     f.pidx[0] = 0;
     f.pidx[1] = 1;
     s->vpSlot = 0;
@@ -719,6 +756,28 @@ int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const 
 int pfs_session_step(pfs_session *s, int n)
 {
     if (!s || n < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "bad session or step count");
+    if (s->lp) {
+        pfs::LpParams lp;
+        lp.dt = s->prm.dt;
+        lp.max_iters = s->prm.max_iters;
+        lp.tol = s->prm.tol;
+        lp.check_every = s->prm.check_every;
+        lp.levels = s->prm.fuse_depth > 0 ? s->prm.fuse_depth : 8;
+        lp.chunk = s->prm.chunk_rows > 0 ? s->prm.chunk_rows : 32;
+        for (int k = 0; k < n; ++k) {
+            pfs::LpOut o;
+            CKS(pfs::lp_step(s->lp, lp, s->st, o));
+            s->stats.sweeps = o.sweeps;
+            s->stats.checks = o.checks;
+            s->stats.rel_residual = o.rel;
+            s->stats.bnorm = o.bnorm;
+            s->stats.capped = o.capped ? 1 : 0;
+            s->stats.steps += 1;
+            s->stats.total_sweeps += o.sweeps;
+            s->stats.cap_hits += o.capped ? 1 : 0;
+        }
+        return PFS_OK;
+    }
     Field &f = s->f;
     const StepCfg c = session_cfg(s);
     for (int k = 0; k < n; ++k) {
@@ -772,14 +831,57 @@ int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, in
         if (tmp) CKS(check_aligned(tmp, "tmp"));
     }
     const int W = s->vpSlot, Z = s->tmpSlot;
-    if (A) CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, f.w, f.h, s->st));
-    if (B) CK(pfs::launch_merge_velocity(B, f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.b, f.ld, f.w, f.h, s->st));
-    if (I && s->ic > 0)
-        CK(pfs::launch_merge_image(I, s->img[s->icur], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
+    if (s->lp) {
+        // (u, v, final pressure, divergence) into both velocity buffers
+        if (A) CKS(pfs::lp_download(s->lp, A, I, s->st));
+        if (B) CKS(pfs::lp_download(s->lp, B, A ? nullptr : I, s->st));
+        if (!A && !B && I) CKS(pfs::lp_download(s->lp, nullptr, I, s->st));
+    } else {
+        if (A) CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, f.w, f.h, s->st));
+        if (B) CK(pfs::launch_merge_velocity(B, f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.b, f.ld, f.w, f.h, s->st));
+        if (I && s->ic > 0)
+            CK(pfs::launch_merge_image(I, s->img[s->icur], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
+    }
     if (where == PFS_HOST) {
         if (vp) CK(cudaMemcpyAsync(vp, A, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
         if (tmp) CK(cudaMemcpyAsync(tmp, B, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
         if (I) CK(cudaMemcpyAsync(image, I, icount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+    }
+    return PFS_OK;
+}
+
+int pfs_session_download_f64(pfs_session *s, double *vp, double *image, int where)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    if (where != PFS_HOST && where != PFS_DEVICE)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "where must be PFS_HOST or PFS_DEVICE");
+    const size_t vcount = (size_t)s->f.w * s->f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
+    double *A = vp, *I = image;
+    if (where == PFS_HOST) {
+        CKS(session_stage(s, (vcount + icount) * sizeof(double)));
+        A = vp ? reinterpret_cast<double *>(s->stage) : nullptr;
+        I = (image && icount) ? reinterpret_cast<double *>(s->stage) + vcount : nullptr;
+    }
+    if (s->lp) {
+        CKS(pfs::lp_download_f64(s->lp, A, I, s->st));
+    } else {
+        // F32 form: the buffers in float32 (vp's velocity, tmp's final pressure), widened
+        Field &f = s->f;
+        float *tmp32 = nullptr;
+        CK(cudaMallocAsync(&tmp32, (vcount * 2 + icount) * sizeof(float), s->st));
+        const int W = s->vpSlot, Z = s->tmpSlot;
+        CK(pfs::launch_merge_velocity(tmp32, f.u[W], f.v[W], f.p[f.pidx[Z]], f.b, f.ld, f.w, f.h, s->st));
+        if (icount)
+            CK(pfs::launch_merge_image(tmp32 + vcount, s->img[s->icur], s->iplane, s->ild, s->iw, s->ih, s->ic,
+                                       s->st));
+        CK(pfs::launch_widen(tmp32, A, vcount, s->st));
+        if (I && icount) CK(pfs::launch_widen(tmp32 + vcount, I, icount, s->st));
+        CK(cudaFreeAsync(tmp32, s->st));
+    }
+    if (where == PFS_HOST) {
+        if (vp) CK(cudaMemcpyAsync(vp, A, vcount * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+        if (I) CK(cudaMemcpyAsync(image, I, icount * sizeof(double), cudaMemcpyDeviceToHost, s->st));
         CK(cudaStreamSynchronize(s->st));
     }
     return PFS_OK;

@@ -2,6 +2,8 @@
 // surface is include/pfs.h).
 #pragma once
 
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -77,6 +79,9 @@ cudaError_t launch_split_image(const float *img, float *planes, size_t plane, in
 cudaError_t launch_merge_image(float *img, const float *planes, size_t plane, int ld, int w, int h, int c,
                                cudaStream_t st);
 
+// float32 -> float64, n elements (out may be null: nothing to do)
+cudaError_t launch_widen(const float *in, double *out, size_t n, cudaStream_t st);
+
 // ---- pressure (sweep_kernels.cu, residual_kernels.cu) ----
 int stream_strip_width(int halo);
 // `done` (may be null): skip the launch when *done != 0
@@ -84,6 +89,11 @@ cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, i
                                 const int *done, cudaStream_t st);
 cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
                                 int h, int levels, int halo, int chunk, const int *done, cudaStream_t st);
+// 16-bit storage, FP32 compute; pin == null means a zero input iterate. levels in [1, 8].
+cudaError_t launch_sweep_stream_bf16(const __nv_bfloat16 *pin, const __nv_bfloat16 *b, __nv_bfloat16 *pout, int ld,
+                                     int w, int h, int levels, int chunk, cudaStream_t st);
+cudaError_t launch_sweep_stream_f16(const __half *pin, const __half *b, __half *pout, int ld, int w, int h,
+                                    int levels, int chunk, cudaStream_t st);
 // sum over cells of r^2, r = b + pL + pR + pT + pB - 4p (exact per cell), into
 // red.result[0]. With `state`: skipped when state->done; otherwise records the
 // check (rel = sqrt(r^2)/sqrt(b^2) from red.result[1]) and marks the solve

@@ -1,0 +1,627 @@
+// Precision forms of the timestep: velocity, image and the pressure
+// correction stored in bf16 / fp16 and computed in FP32, with the pressure
+// itself and its residual kept in FP64 (mixed-precision iterative
+// refinement); and an all-FP64 form, the FP64 run of the same method used to
+// measure every form's error.
+//
+// The method is the reference's (src/fluid.cpp:298-320) in the configuration
+// viscosity 0 with an even diffusion count, where its buffer roles reduce to:
+// advect the velocity; divergence of the advected velocity; Jacobi on the
+// pressure from the previous step's final pressure; projection with the final
+// pressure; image advection with the projected velocity.
+//
+// Iterative refinement keeps the method: with x the FP64 pressure and
+// r = b - A x, m Jacobi sweeps on A e = r started from e = 0 give
+// x + e = m Jacobi sweeps on A x = b started from x, because a Jacobi sweep is
+// affine (x' = M x + D^-1 b). Only the rounding differs: x, r and the update
+// x += e are FP64; the sweeps on e store e and r in 16 bits (r scaled by
+// 1 / max|r| so it fills the 16-bit range) and compute in FP32.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <type_traits>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "precision.h"
+#include "reduce.cuh"
+#include "storage.cuh"
+
+namespace pfs {
+namespace {
+
+// ---- arithmetic in the compute type: one rounding per operation ----
+template <typename C>
+struct Ar;
+template <>
+struct Ar<float> {
+    __device__ static float add(float a, float b) { return __fadd_rn(a, b); }
+    __device__ static float sub(float a, float b) { return __fsub_rn(a, b); }
+    __device__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+    __device__ static float div(float a, float b) { return __fdiv_rn(a, b); }
+    __device__ static float fmod_(float a, float b) { return fmodf(a, b); }
+    __device__ static int trunc(float a) { return __float2int_rz(a); }
+};
+template <>
+struct Ar<double> {
+    __device__ static double add(double a, double b) { return __dadd_rn(a, b); }
+    __device__ static double sub(double a, double b) { return __dsub_rn(a, b); }
+    __device__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+    __device__ static double div(double a, double b) { return __ddiv_rn(a, b); }
+    __device__ static double fmod_(double a, double b) { return fmod(a, b); }
+    __device__ static int trunc(double a) { return __double2int_rz(a); }
+};
+
+// Storage load/store in the compute type (double storage is only used with
+// double compute).
+template <typename T, typename C>
+__device__ __forceinline__ C ldv(const T *p)
+{
+    if constexpr (std::is_same<T, double>::value) return (C)*p;
+    else return (C)Store<T>::to_f(*p);
+}
+template <typename T, typename C>
+__device__ __forceinline__ void stv(T *p, C v)
+{
+    if constexpr (std::is_same<T, double>::value) *p = (double)v;
+    else *p = Store<T>::from_f((float)v);
+}
+
+template <typename C>
+__device__ __forceinline__ C fmod_small_t(C x, C n)
+{
+    if (x >= n) return x == (C)2 * n ? (C)0 : Ar<C>::sub(x, n);
+    if (x == -n) return -(C)0;
+    return x;
+}
+// fmod(fmod(x, n) + n, n) (src/fluid.cpp:48-49), exact fast path as wrap_coord.
+template <typename C>
+__device__ __forceinline__ C wrap_t(C x, C n)
+{
+    if (x >= -n && x < (C)2 * n) return fmod_small_t(Ar<C>::add(fmod_small_t(x, n), n), n);
+    return Ar<C>::fmod_(Ar<C>::add(Ar<C>::fmod_(x, n), n), n);
+}
+
+template <typename C>
+__device__ __forceinline__ C bilerp_t(C sx, C sy, C f00, C f10, C f01, C f11)
+{
+    const C ox = Ar<C>::sub((C)1, sx), oy = Ar<C>::sub((C)1, sy);
+    const C a = Ar<C>::mul(Ar<C>::mul(ox, oy), f00);
+    const C b = Ar<C>::mul(Ar<C>::mul(sx, oy), f10);
+    const C c = Ar<C>::mul(Ar<C>::mul(ox, sy), f01);
+    const C d = Ar<C>::mul(Ar<C>::mul(sx, sy), f11);
+    return Ar<C>::add(Ar<C>::add(Ar<C>::add(a, b), c), d);
+}
+
+template <typename C>
+struct CornersT {
+    int i0, i1, j0, j1;
+    C sx, sy;
+};
+
+template <typename C>
+__device__ __forceinline__ CornersT<C> backtrace_t(int i, int j, C kx, C ky, C u, C v, int w, int h)
+{
+    const C fw = (C)w, fh = (C)h;
+    C xp = Ar<C>::sub((C)i, Ar<C>::div(Ar<C>::mul(kx, u), fw));
+    C yp = Ar<C>::sub((C)j, Ar<C>::div(Ar<C>::mul(ky, v), fh));
+    xp = wrap_t(xp, fw);
+    yp = wrap_t(yp, fh);
+    CornersT<C> c;
+    c.i0 = min(max(Ar<C>::trunc(xp), 0), w - 1);
+    c.j0 = min(max(Ar<C>::trunc(yp), 0), h - 1);
+    c.i1 = (c.i0 + 1) % w;
+    c.j1 = (c.j0 + 1) % h;
+    c.sx = Ar<C>::sub(xp, (C)c.i0);
+    c.sy = Ar<C>::sub(yp, (C)c.j0);
+    return c;
+}
+
+__device__ __forceinline__ int wm_(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wp_(int i, int n) { return i + 1 == n ? 0 : i + 1; }
+
+constexpr int kBX = 32, kBY = 8;
+inline dim3 g2(int w, int h) { return dim3((w + kBX - 1) / kBX, (h + kBY - 1) / kBY); }
+
+// src/fluid.cpp:24-70
+template <typename T, typename C>
+__global__ void k_lp_advect(const T *__restrict__ u, const T *__restrict__ v, T *__restrict__ uo, T *__restrict__ vo,
+                            int ld, int w, int h, C dt)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t o = (size_t)j * ld + i;
+    const CornersT<C> c = backtrace_t<C>(i, j, dt, dt, ldv<T, C>(u + o), ldv<T, C>(v + o), w, h);
+    const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
+    stv<T, C>(uo + o, bilerp_t<C>(c.sx, c.sy, ldv<T, C>(u + r0 + c.i0), ldv<T, C>(u + r0 + c.i1), ldv<T, C>(u + r1 + c.i0),
+                                 ldv<T, C>(u + r1 + c.i1)));
+    stv<T, C>(vo + o, bilerp_t<C>(c.sx, c.sy, ldv<T, C>(v + r0 + c.i0), ldv<T, C>(v + r0 + c.i1), ldv<T, C>(v + r1 + c.i0),
+                                 ldv<T, C>(v + r1 + c.i1)));
+}
+
+// src/fluid.cpp:218-237; also sum b^2 (slot 1).
+template <typename T, typename B, typename C>
+__global__ void __launch_bounds__(256) k_lp_divergence(const T *__restrict__ u, const T *__restrict__ v,
+                                                       B *__restrict__ b, int ld, int w, int h, C gamma, Reduce red)
+{
+    FFAcc accf;
+    double accd = 0.0;
+    for (int j = blockIdx.x; j < h; j += gridDim.x) {
+        const size_t r = (size_t)j * ld, rm = (size_t)wm_(j, h) * ld, rp = (size_t)wp_(j, h) * ld;
+        for (int i = threadIdx.x; i < w; i += blockDim.x) {
+            const C du = Ar<C>::sub(ldv<T, C>(u + r + wp_(i, w)), ldv<T, C>(u + r + wm_(i, w)));
+            const C dv = Ar<C>::sub(ldv<T, C>(v + rp + i), ldv<T, C>(v + rm + i));
+            const C bv = Ar<C>::mul(gamma, Ar<C>::add(du, dv));
+            b[r + i] = (B)bv;
+            if constexpr (std::is_same<C, double>::value) accd = __fma_rn(bv, bv, accd);
+            else acc_square(accf, bv);
+        }
+    }
+    reduce_blocks(std::is_same<C, double>::value ? accd : accf.value(), red, 1);
+}
+
+// Refinement: x_out = x_in + e / scale (e may be null: no correction yet);
+// r = b - A x_out in FP64 per cell, stored as float; sum r^2 (slot 0) and
+// max |r| (as float bits, atomicMax).
+template <typename T>
+__global__ void __launch_bounds__(256) k_lp_refine(const double *__restrict__ x_in, const T *__restrict__ e,
+                                                   const double *__restrict__ escale, const float *__restrict__ b,
+                                                   double *__restrict__ x_out, float *__restrict__ rout, int ld,
+                                                   int w, int h, Reduce red, unsigned *maxabs)
+{
+    const double inv = e ? 1.0 / *escale : 0.0;
+    double acc = 0.0;
+    unsigned mx = 0u;
+    for (int j = blockIdx.x; j < h; j += gridDim.x) {
+        const size_t r = (size_t)j * ld, rm = (size_t)wm_(j, h) * ld, rp = (size_t)wp_(j, h) * ld;
+        for (int i = threadIdx.x; i < w; i += blockDim.x) {
+            const int im = wm_(i, w), ip = wp_(i, w);
+            auto xn = [&](size_t k) {
+                return e ? __fma_rn((double)Store<T>::to_f(e[k]), inv, x_in[k]) : x_in[k];
+            };
+            const double xc = xn(r + i);
+            double q = __dadd_rn((double)b[r + i], xn(r + im));
+            q = __dadd_rn(q, xn(r + ip));
+            q = __dadd_rn(q, xn(rm + i));
+            q = __dadd_rn(q, xn(rp + i));
+            q = __dsub_rn(q, __dmul_rn(4.0, xc));
+            x_out[r + i] = xc;
+            const float qf = (float)q;
+            rout[r + i] = qf;
+            mx = max(mx, __float_as_uint(fabsf(qf)));
+            acc = __fma_rn(q, q, acc);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(maxabs, mx);
+    reduce_blocks(acc, red, 0);
+}
+
+// r (float) -> 16-bit right-hand side scaled by 1 / max|r|; records the scale.
+template <typename T>
+__global__ void k_lp_scale(const float *__restrict__ r, T *__restrict__ rt, size_t n, const unsigned *maxabs,
+                           double *escale)
+{
+    const float m = __uint_as_float(*maxabs);
+    const float s = m > 0.0f ? 1.0f / m : 1.0f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *escale = (double)s;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        rt[k] = Store<T>::from_f(r[k] * s);
+}
+
+// FP64 form: one Jacobi sweep (src/fluid.cpp:239-257 in double).
+__global__ void k_f64_sweep(const double *__restrict__ pin, const double *__restrict__ b, double *__restrict__ pout,
+                            int ld, int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t r = (size_t)j * ld;
+    const double s = __dadd_rn(__dadd_rn(__dadd_rn(pin[r + wm_(i, w)], pin[r + wp_(i, w)]),
+                                         pin[(size_t)wm_(j, h) * ld + i]),
+                               pin[(size_t)wp_(j, h) * ld + i]);
+    pout[r + i] = __ddiv_rn(__dadd_rn(s, b[r + i]), 4.0);
+}
+
+// FP64 form: residual exactly as the oracle evaluates it, sum r^2 (slot 0).
+__global__ void __launch_bounds__(256) k_f64_residual(const double *__restrict__ p, const double *__restrict__ b,
+                                                      int ld, int w, int h, Reduce red)
+{
+    double acc = 0.0;
+    for (int j = blockIdx.x; j < h; j += gridDim.x) {
+        const size_t r = (size_t)j * ld, rm = (size_t)wm_(j, h) * ld, rp = (size_t)wp_(j, h) * ld;
+        for (int i = threadIdx.x; i < w; i += blockDim.x) {
+            double q = __dadd_rn(b[r + i], p[r + wm_(i, w)]);
+            q = __dadd_rn(q, p[r + wp_(i, w)]);
+            q = __dadd_rn(q, p[rm + i]);
+            q = __dadd_rn(q, p[rp + i]);
+            q = __dsub_rn(q, __dmul_rn(4.0, p[r + i]));
+            acc = __fma_rn(q, q, acc);
+        }
+    }
+    reduce_blocks(acc, red, 0);
+}
+
+// Projection (src/fluid.cpp:269-296) with the FP64 pressure: the gradient is
+// formed in C from the pressure values, ((pR - pL) * dt) / 2.
+template <typename C>
+__device__ __forceinline__ void lp_grad(const double *__restrict__ x, int ld, int w, int h, C dt, int i, int j, C &gx,
+                                        C &gy)
+{
+    const size_t r = (size_t)j * ld;
+    const C dx = (C)(x[r + wp_(i, w)] - x[r + wm_(i, w)]);
+    const C dy = (C)(x[(size_t)wp_(j, h) * ld + i] - x[(size_t)wm_(j, h) * ld + i]);
+    gx = Ar<C>::div(Ar<C>::mul(dx, dt), (C)2);
+    gy = Ar<C>::div(Ar<C>::mul(dy, dt), (C)2);
+}
+
+template <typename T, typename C>
+__global__ void k_lp_project(const T *__restrict__ ua, const T *__restrict__ va, const double *__restrict__ x,
+                             T *__restrict__ u, T *__restrict__ v, int ld, int w, int h, C dt)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    C gx, gy;
+    lp_grad<C>(x, ld, w, h, dt, i, j, gx, gy);
+    const size_t o = (size_t)j * ld + i;
+    stv<T, C>(u + o, Ar<C>::sub(ldv<T, C>(ua + o), gx));
+    stv<T, C>(v + o, Ar<C>::sub(ldv<T, C>(va + o), gy));
+}
+
+// src/fluid.cpp:72-127 on planar T fields.
+template <typename T, typename C>
+__global__ void k_lp_advect_image(const T *__restrict__ img, T *__restrict__ imgo, size_t plane, int ild, int iw,
+                                  int ih, int c, const T *__restrict__ u, const T *__restrict__ v, int vld, int vw,
+                                  int vh, C viw, C vih, C kx, C ky)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= iw || j >= ih) return;
+    const int vi = min(Ar<C>::trunc(Ar<C>::mul((C)i, viw)), vw - 1);
+    const int vj = min(Ar<C>::trunc(Ar<C>::mul((C)j, vih)), vh - 1);
+    const size_t vo = (size_t)vj * vld + vi;
+    const CornersT<C> k = backtrace_t<C>(i, j, kx, ky, ldv<T, C>(u + vo), ldv<T, C>(v + vo), iw, ih);
+    const size_t r0 = (size_t)k.j0 * ild, r1 = (size_t)k.j1 * ild, o = (size_t)j * ild + i;
+    for (int ch = 0; ch < c; ++ch) {
+        const T *s = img + ch * plane;
+        stv<T, C>(imgo + ch * plane + o, bilerp_t<C>(k.sx, k.sy, ldv<T, C>(s + r0 + k.i0), ldv<T, C>(s + r0 + k.i1),
+                                                    ldv<T, C>(s + r1 + k.i0), ldv<T, C>(s + r1 + k.i1)));
+    }
+}
+
+// interleaved float32 (h, w, nch) channel k -> planar T / double
+template <typename T>
+__global__ void k_lp_split(const float *__restrict__ buf, int k, int nch, T *__restrict__ plane, int ld, int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const float x = buf[((size_t)j * w + i) * nch + k];
+    if constexpr (std::is_same<T, double>::value) plane[(size_t)j * ld + i] = (double)x;
+    else plane[(size_t)j * ld + i] = Store<T>::from_f(x);
+}
+
+// planar T / double -> interleaved O (float or double) channel k
+template <typename T, typename O>
+__global__ void k_lp_merge(O *__restrict__ buf, int k, int nch, const T *__restrict__ plane, int ld, int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    double x;
+    if constexpr (std::is_same<T, double>::value) x = plane[(size_t)j * ld + i];
+    else if constexpr (std::is_same<T, float>::value) x = (double)plane[(size_t)j * ld + i];
+    else x = (double)Store<T>::to_f(plane[(size_t)j * ld + i]);
+    buf[((size_t)j * w + i) * nch + k] = (O)x;
+}
+
+inline int rup(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+// =============================================================================================
+// Host side
+
+struct LpState {
+    int form = 0;  // PFS_PREC_*
+    int w = 0, h = 0, ld = 0, iw = 0, ih = 0, ic = 0, ild = 0;
+    size_t plane = 0, iplane = 0;
+    size_t tbytes = 0;  // bytes per element of the velocity / image / correction storage
+    // velocity (T) current and advected; image (T) x2; pressure x (double) x2;
+    // b (float, or double in the FP64 form); r (float) and 16-bit r, e x2
+    void *u = nullptr, *v = nullptr, *ua = nullptr, *va = nullptr, *img[2] = {nullptr, nullptr};
+    double *x[2] = {nullptr, nullptr};
+    void *b = nullptr;
+    float *r = nullptr;
+    void *rt = nullptr, *e[2] = {nullptr, nullptr};
+    int xcur = 0, icur = 0;
+    void *mem = nullptr;
+    double *rmem = nullptr;
+    unsigned *maxabs = nullptr;
+    double *escale = nullptr;
+    double *hres = nullptr;
+    Reduce red{};
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+namespace {
+
+int lp_fail(int code, const char *msg) { return record_error(code, msg); }
+
+#define LCK(x)                                                     \
+    do {                                                           \
+        cudaError_t e_ = (x);                                      \
+        if (e_ != cudaSuccess) return lp_fail(PFS_ERR_CUDA, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T, typename C>
+int lp_velocity_and_image(LpState &s, const LpParams &p, cudaStream_t st, double *xfinal)
+{
+    const int w = s.w, h = s.h, ld = s.ld;
+    T *u = (T *)s.u, *v = (T *)s.v, *ua = (T *)s.ua, *va = (T *)s.va;
+    k_lp_project<T, C><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(ua, va, xfinal, u, v, ld, w, h, (C)p.dt);
+    LCK(launched());
+    if (s.ic > 0) {
+        const C viw = (C)w / (C)s.iw, vih = (C)h / (C)s.ih;
+        const C kx = (C)p.dt / viw, ky = (C)p.dt / vih;
+        k_lp_advect_image<T, C><<<g2(s.iw, s.ih), dim3(kBX, kBY), 0, st>>>(
+            (T *)s.img[s.icur], (T *)s.img[1 - s.icur], s.iplane, s.ild, s.iw, s.ih, s.ic, u, v, ld, w, h, viw, vih, kx,
+            ky);
+        LCK(launched());
+        s.icur = 1 - s.icur;
+    }
+    return PFS_OK;
+}
+
+double rel_of(double rr, double bb) { return bb > 0.0 ? std::sqrt(rr) / std::sqrt(bb) : std::sqrt(rr); }
+
+// One step of a 16-bit form.
+template <typename T>
+int lp_step16(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
+{
+    const int w = s.w, h = s.h, ld = s.ld;
+    k_lp_advect<T, float><<<g2(w, h), dim3(kBX, kBY), 0, st>>>((T *)s.u, (T *)s.v, (T *)s.ua, (T *)s.va, ld, w, h,
+                                                                p.dt);
+    LCK(launched());
+    const float gamma = (float)(-1.0 / (double)p.dt);
+    k_lp_divergence<T, float, float><<<s.red.nblocks, 256, 0, st>>>((T *)s.ua, (T *)s.va, (float *)s.b, ld, w, h,
+                                                                    gamma, s.red);
+    LCK(launched());
+    const int m = p.check_every > 0 ? p.check_every : 32;  // sweeps between refinements
+    int S = 0;
+    T *ecur = nullptr;  // correction of the last inner solve (null before the first)
+    o.checks = 0;
+    for (;;) {
+        // x_new = x + e/scale; r = b - A x_new (FP64); |r| stats
+        LCK(cudaMemsetAsync(s.maxabs, 0, sizeof(unsigned), st));
+        k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], ecur, s.escale, (const float *)s.b,
+                                                       s.x[1 - s.xcur], s.r, ld, w, h, s.red, s.maxabs);
+        LCK(launched());
+        s.xcur = 1 - s.xcur;
+        LCK(cudaMemcpyAsync(s.hres, s.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        LCK(cudaStreamSynchronize(st));
+        o.checks++;
+        o.rel = rel_of(s.hres[0], s.hres[1]);
+        o.bnorm = std::sqrt(s.hres[1]);
+        const bool resid = p.tol > 0.0;
+        if ((resid && o.rel <= p.tol) || S >= p.max_iters) break;
+        // inner solve: n sweeps on A e = r from e = 0, 16-bit storage
+        const int n = std::min(m, p.max_iters - S);
+        k_lp_scale<T><<<s.red.nblocks, 256, 0, st>>>(s.r, (T *)s.rt, s.plane, s.maxabs, s.escale);
+        LCK(launched());
+        int done = 0, cur = -1;
+        while (done < n) {
+            const int L = std::min(p.levels, n - done);
+            const int out = (cur == 0) ? 1 : 0;
+            const T *in = cur < 0 ? nullptr : (const T *)s.e[cur];
+            cudaError_t e;
+            if constexpr (std::is_same<T, __nv_bfloat16>::value)
+                e = launch_sweep_stream_bf16(in, (const T *)s.rt, (T *)s.e[out], ld, w, h, L, p.chunk, st);
+            else
+                e = launch_sweep_stream_f16(in, (const T *)s.rt, (T *)s.e[out], ld, w, h, L, p.chunk, st);
+            LCK(e);
+            cur = out;
+            done += L;
+        }
+        ecur = (T *)s.e[cur];
+        S += n;
+    }
+    o.sweeps = S;
+    o.capped = p.tol > 0.0 && !(o.rel <= p.tol);
+    return lp_velocity_and_image<T, float>(s, p, st, s.x[s.xcur]);
+}
+
+// One step of the FP64 form: plain Jacobi on x in FP64, checks every m sweeps.
+int lp_step64(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
+{
+    const int w = s.w, h = s.h, ld = s.ld;
+    const double dt = (double)p.dt;
+    k_lp_advect<double, double><<<g2(w, h), dim3(kBX, kBY), 0, st>>>((double *)s.u, (double *)s.v, (double *)s.ua,
+                                                                      (double *)s.va, ld, w, h, dt);
+    LCK(launched());
+    const double gamma = -1.0 / dt;
+    k_lp_divergence<double, double, double><<<s.red.nblocks, 256, 0, st>>>((double *)s.ua, (double *)s.va,
+                                                                           (double *)s.b, ld, w, h, gamma, s.red);
+    LCK(launched());
+    const bool resid = p.tol > 0.0;
+    int S = 0;
+    o.checks = 0;
+    while (S < p.max_iters) {
+        int stop = p.max_iters;
+        if (resid && p.check_every > 0) stop = std::min(p.max_iters, (S / p.check_every + 1) * p.check_every);
+        for (; S < stop; ++S) {
+            k_f64_sweep<<<g2(w, h), dim3(kBX, kBY), 0, st>>>(s.x[s.xcur], (double *)s.b, s.x[1 - s.xcur], ld, w, h);
+            LCK(launched());
+            s.xcur = 1 - s.xcur;
+        }
+        if (!resid) break;
+        k_f64_residual<<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], (double *)s.b, ld, w, h, s.red);
+        LCK(launched());
+        LCK(cudaMemcpyAsync(s.hres, s.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        LCK(cudaStreamSynchronize(st));
+        o.checks++;
+        o.rel = rel_of(s.hres[0], s.hres[1]);
+        o.bnorm = std::sqrt(s.hres[1]);
+        if (o.rel <= p.tol) break;
+    }
+    o.sweeps = S;
+    o.capped = resid && S == p.max_iters && !(o.rel <= p.tol);
+    return lp_velocity_and_image<double, double>(s, p, st, s.x[s.xcur]);
+}
+
+template <typename T>
+int lp_upload_t(LpState &s, const float *A, const float *B, const float *I, cudaStream_t st)
+{
+    const int w = s.w, h = s.h, ld = s.ld;
+    k_lp_split<T><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(A, 0, 4, (T *)s.u, ld, w, h);
+    k_lp_split<T><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(A, 1, 4, (T *)s.v, ld, w, h);
+    k_lp_split<double><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(B, 2, 4, s.x[0], ld, w, h);
+    LCK(launched(3));
+    s.xcur = 0;
+    for (int k = 0; k < s.ic; ++k) {
+        k_lp_split<T><<<g2(s.iw, s.ih), dim3(kBX, kBY), 0, st>>>(I, k, s.ic, (T *)s.img[0] + k * s.iplane, s.ild, s.iw,
+                                                                 s.ih);
+        LCK(launched());
+    }
+    s.icur = 0;
+    return PFS_OK;
+}
+
+template <typename T, typename O>
+int lp_download_t(LpState &s, O *vp, O *img, cudaStream_t st)
+{
+    const int w = s.w, h = s.h, ld = s.ld;
+    if (vp) {
+        k_lp_merge<T, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 0, 4, (T *)s.u, ld, w, h);
+        k_lp_merge<T, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 1, 4, (T *)s.v, ld, w, h);
+        k_lp_merge<double, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 2, 4, s.x[s.xcur], ld, w, h);
+        if (s.form == PFS_PREC_F64)
+            k_lp_merge<double, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 3, 4, (double *)s.b, ld, w, h);
+        else
+            k_lp_merge<float, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 3, 4, (float *)s.b, ld, w, h);
+        LCK(launched(4));
+    }
+    if (img)
+        for (int k = 0; k < s.ic; ++k) {
+            k_lp_merge<T, O><<<g2(s.iw, s.ih), dim3(kBX, kBY), 0, st>>>(img, k, s.ic, (T *)s.img[s.icur] + k * s.iplane,
+                                                                        s.ild, s.iw, s.ih);
+            LCK(launched());
+        }
+    return PFS_OK;
+}
+
+}  // namespace
+
+int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
+{
+    *out = nullptr;
+    LpState *s = new (std::nothrow) LpState();
+    if (!s) return lp_fail(PFS_ERR_CUDA, "out of host memory");
+    s->form = form;
+    s->w = w;
+    s->h = h;
+    s->ld = rup(w, 32);
+    s->plane = (size_t)s->ld * h;
+    s->iw = iw;
+    s->ih = ih;
+    s->ic = ic;
+    s->ild = rup(std::max(iw, 1), 32);
+    s->iplane = (size_t)s->ild * ih;
+    s->tbytes = form == PFS_PREC_F64 ? 8 : 2;
+    const size_t P = s->plane, TB = s->tbytes;
+    const size_t bbytes = (form == PFS_PREC_F64 ? 8 : 4) * P;
+    // u v ua va (T) | x x (double) | b | r (float) | rt e e (T) | image x2 (T)
+    const size_t total = 4 * TB * P + 2 * 8 * P + bbytes + 4 * P + 3 * TB * P + 2 * TB * s->iplane * ic + 6 * 256;
+    cudaError_t e = cudaMalloc(&s->mem, total);
+    if (e == cudaSuccess) e = cudaMemset(s->mem, 0, total);
+    if (e != cudaSuccess) {
+        delete s;
+        return lp_fail(PFS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    unsigned char *q = (unsigned char *)s->mem;
+    auto take = [&](size_t n) {
+        void *r = q;
+        q += (n + 255) / 256 * 256;
+        return r;
+    };
+    s->u = take(TB * P);
+    s->v = take(TB * P);
+    s->ua = take(TB * P);
+    s->va = take(TB * P);
+    s->x[0] = (double *)take(8 * P);
+    s->x[1] = (double *)take(8 * P);
+    s->b = take(bbytes);
+    s->r = (float *)take(4 * P);
+    s->rt = take(TB * P);
+    s->e[0] = take(TB * P);
+    s->e[1] = take(TB * P);
+    s->img[0] = take(TB * s->iplane * ic);
+    s->img[1] = take(TB * s->iplane * ic);
+    const int nb = kReduceBlocks;
+    e = cudaMalloc(&s->rmem, (2 * nb + 2) * sizeof(double) + 16 + 16);
+    if (e == cudaSuccess) e = cudaMemset(s->rmem, 0, (2 * nb + 2) * sizeof(double) + 32);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->hres, 2 * sizeof(double));
+    if (e != cudaSuccess) {
+        lp_destroy(s);
+        return lp_fail(PFS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    s->red.partials = s->rmem;
+    s->red.result = s->rmem + 2 * nb;
+    s->red.ticket = reinterpret_cast<unsigned *>(s->rmem + 2 * nb + 2);
+    s->red.nblocks = nb;
+    s->maxabs = s->red.ticket + 2;
+    s->escale = reinterpret_cast<double *>(s->rmem + 2 * nb + 2) + 1;
+    *out = s;
+    return PFS_OK;
+}
+
+void lp_destroy(LpState *s)
+{
+    if (!s) return;
+    if (s->mem) cudaFree(s->mem);
+    if (s->rmem) cudaFree(s->rmem);
+    if (s->hres) cudaFreeHost(s->hres);
+    if (s->stage) cudaFree(s->stage);
+    delete s;
+}
+
+int lp_upload(LpState *s, const float *vp_dev, const float *tmp_dev, const float *img_dev, cudaStream_t st)
+{
+    switch (s->form) {
+    case PFS_PREC_BF16: return lp_upload_t<__nv_bfloat16>(*s, vp_dev, tmp_dev, img_dev, st);
+    case PFS_PREC_F16: return lp_upload_t<__half>(*s, vp_dev, tmp_dev, img_dev, st);
+    case PFS_PREC_F64: return lp_upload_t<double>(*s, vp_dev, tmp_dev, img_dev, st);
+    default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
+    }
+}
+
+int lp_step(LpState *s, const LpParams &p, cudaStream_t st, LpOut &o)
+{
+    switch (s->form) {
+    case PFS_PREC_BF16: return lp_step16<__nv_bfloat16>(*s, p, st, o);
+    case PFS_PREC_F16: return lp_step16<__half>(*s, p, st, o);
+    case PFS_PREC_F64: return lp_step64(*s, p, st, o);
+    default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
+    }
+}
+
+int lp_download(LpState *s, float *vp_dev, float *img_dev, cudaStream_t st)
+{
+    switch (s->form) {
+    case PFS_PREC_BF16: return lp_download_t<__nv_bfloat16, float>(*s, vp_dev, img_dev, st);
+    case PFS_PREC_F16: return lp_download_t<__half, float>(*s, vp_dev, img_dev, st);
+    case PFS_PREC_F64: return lp_download_t<double, float>(*s, vp_dev, img_dev, st);
+    default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
+    }
+}
+
+int lp_download_f64(LpState *s, double *vp_dev, double *img_dev, cudaStream_t st)
+{
+    switch (s->form) {
+    case PFS_PREC_BF16: return lp_download_t<__nv_bfloat16, double>(*s, vp_dev, img_dev, st);
+    case PFS_PREC_F16: return lp_download_t<__half, double>(*s, vp_dev, img_dev, st);
+    case PFS_PREC_F64: return lp_download_t<double, double>(*s, vp_dev, img_dev, st);
+    default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
+    }
+}
+
+}  // namespace pfs

@@ -1,0 +1,101 @@
+// Deterministic grid reductions and error-free float arithmetic shared by
+// the step kernels and the precision-form kernels.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pfs {
+namespace {
+
+// Block sum of `acc`, written to red.partials[blockIdx.x * 2 + slot]; the last
+// block to finish adds the partials in block order into red.result[slot] and
+// re-arms that slot's ticket (one ticket per slot, so two reductions in one
+// kernel do not mix their counts). The order of additions is fixed, so the sum is
+// reproducible run to run.
+__device__ void reduce_blocks(double acc, const Reduce &red, int slot, SolveState *state = nullptr,
+                              int sweeps_here = 0, double tol = 0.0)
+{
+    __shared__ double ws[32];
+    __shared__ bool last;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) ws[wid] = acc;
+    __syncthreads();
+    if (wid == 0) {
+        acc = lane < nw ? ws[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            red.partials[blockIdx.x * 2 + slot] = acc;
+            __threadfence();
+            last = atomicAdd(red.ticket + slot, 1u) == gridDim.x - 1;
+        }
+    }
+    __syncthreads();
+    if (last && wid == 0) {
+        __threadfence();
+        double s = 0.0;
+        for (int k = lane; k < (int)gridDim.x; k += 32) s += __ldcg(red.partials + k * 2 + slot);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            red.result[slot] = s;
+            red.ticket[slot] = 0u;
+            if (state) {
+                const double bb = red.result[1];
+                const double rel = bb > 0.0 ? __dsqrt_rn(s) / __dsqrt_rn(bb) : __dsqrt_rn(s);
+                state->rr = s;
+                state->bb = bb;
+                state->rel = rel;
+                state->checks += 1;
+                if (rel <= tol) {
+                    state->sweeps = sweeps_here;
+                    state->done = 1;
+                }
+            }
+        }
+    }
+}
+
+// Error-free float transformations (Knuth's TwoSum, and the product error
+// from one fused multiply-add) used to evaluate the residual exactly without
+// FP64 arithmetic per cell: on GB300 the FP64 pipe runs at a small fraction
+// of the FP32 rate.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+// Per-thread sum of squares kept as an unevaluated pair hi + lo of floats
+// (about 48 significant bits); converted to double once per thread, and the
+// block and grid sums are FP64.
+struct FFAcc {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float a, float a_lo)
+    {
+        const FF s = two_sum(hi, a);
+        const float e = __fadd_rn(s.lo, __fadd_rn(lo, a_lo));
+        hi = __fadd_rn(s.hi, e);
+        lo = __fsub_rn(e, __fsub_rn(hi, s.hi));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// x^2 as hi + lo: the product and its exact rounding error (one FMA).
+__device__ __forceinline__ void acc_square(FFAcc &acc, float x)
+{
+    const float sq = __fmul_rn(x, x);
+    acc.add(sq, __fmaf_rn(x, x, -sq));
+}
+
+}  // namespace
+}  // namespace pfs

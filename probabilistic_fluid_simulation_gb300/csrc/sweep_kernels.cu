@@ -18,6 +18,7 @@
 // Jacobi sweep is order-independent, so any fusion depth gives the same bits.
 #include "common.cuh"
 #include "kernels.h"
+#include "storage.cuh"
 
 namespace pfs {
 
@@ -63,11 +64,12 @@ __device__ __forceinline__ float4 jacobi4(const float4 &c, const float4 &up, con
     return make_float4(a.x, a.y, z.x, z.y);
 }
 
+template <typename T>
 struct StreamArgs {
-    const float *pin;
-    const float *b;
-    float *pout;
-    float *pprev;  // receives level L-1 (the second-to-last iterate) when non-null
+    const T *pin;     // null: the input iterate is all zeros
+    const T *b;
+    T *pout;
+    T *pprev;         // receives level L-1 (the second-to-last iterate) when non-null
     const int *done;  // solve already converged: return at once
     int ld, w, h;
     int nsx, nwork, chunk;
@@ -84,35 +86,48 @@ constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
 // Unrolling the row loop by U = lcm(3, L+1) makes every ring index a
 // compile-time register name: no register moves, one shared-memory read of b
 // per row instead of one per level.
-template <int L>
+template <typename T, int L>
 struct Ring {
     static constexpr int NB = L + 1;
     static constexpr int U = 3 * NB / gcd_c(3, NB);
-    static constexpr int floats4_per_warp = 2 * kRP * 32;  // p and b prefetch rings
-    static constexpr int bytes_per_block = 4 * floats4_per_warp * 16;
+    static constexpr int vecs_per_warp = 2 * kRP * 32;  // p and b prefetch rings, one vector per lane and row
+    static constexpr int bytes_per_block = 4 * vecs_per_warp * Store<T>::vec_bytes;
 };
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem);
+template <>
+__device__ __forceinline__ void cp_async<16>(void *smem, const void *gmem)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <>
+__device__ __forceinline__ void cp_async<8>(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+template <typename T>
 struct Cursor {
-    const float *gp, *gb;  // next row to prefetch (p and b planes, lane column)
+    const T *gp, *gb;      // next row to prefetch (p and b planes, lane column)
     int ld_row;            // its row index (wrapped)
     long long st_off;      // offset of the level-L row of this step, in floats from the lane column
     int st_rel;            // that row minus y0 (stored when 0 <= st_rel < rows)
 };
 
 // Issue the cp.async of the next row into ring slot `slot` of p and b.
-__device__ __forceinline__ void prefetch_row(Cursor &cu, float4 *pr, float4 *br, int slot, const StreamArgs &a)
+template <typename T>
+__device__ __forceinline__ void prefetch_row(Cursor<T> &cu, typename Store<T>::Vec *pr, typename Store<T>::Vec *br,
+                                             int slot, const StreamArgs<T> &a)
 {
-    cp_async16(pr + slot * 32, cu.gp);
-    cp_async16(br + slot * 32, cu.gb);
+    constexpr int VB = Store<T>::vec_bytes;
+    if (a.pin) cp_async<VB>(pr + slot * 32, cu.gp);
+    cp_async<VB>(br + slot * 32, cu.gb);
     if (++cu.ld_row == a.h) {
         cu.ld_row = 0;
         cu.gp -= (size_t)(a.h - 1) * a.ld;
@@ -125,11 +140,12 @@ __device__ __forceinline__ void prefetch_row(Cursor &cu, float4 *pr, float4 *br,
 
 // One row step t of the pipeline (load row y = ybeg + t); K = t mod U is a
 // compile-time constant, so R[K % 3]... and bq[...] name fixed registers.
-template <int L, bool PREV, int K>
-__device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[L + 1], float4 *pr, float4 *br,
-                                            Cursor &cu, const StreamArgs &a, int nsteps, int rows, float *out,
-                                            float *outp)
+template <typename T, int L, bool PREV, int K>
+__device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[L + 1],
+                                            typename Store<T>::Vec *pr, typename Store<T>::Vec *br, Cursor<T> &cu,
+                                            const StreamArgs<T> &a, int nsteps, int rows, T *out, T *outp)
 {
+    using V = typename Store<T>::Vec;
     constexpr int NB = L + 1;
     float4(&P)[L] = R[K % 3];
     float4(&Cur)[L] = R[(K + 1) % 3];
@@ -137,8 +153,8 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
     if (t + kRP - 1 < nsteps) prefetch_row(cu, pr, br, (t + kRP - 1) & (kRP - 1), a);
     cp_async_commit();
     cp_async_wait<kRP - 1>();  // row t has landed
-    N[0] = pr[(t & (kRP - 1)) * 32];
-    bq[K % NB] = br[(t & (kRP - 1)) * 32];  // b of row y, first used at the next step
+    N[0] = a.pin ? Store<T>::to_f4(pr[(t & (kRP - 1)) * 32]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    bq[K % NB] = Store<T>::to_f4(br[(t & (kRP - 1)) * 32]);  // b of row y, first used at the next step
     float4 top;
 #pragma unroll
     for (int s = 0; s < L; ++s) {
@@ -147,22 +163,22 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
         if (s + 1 < L) N[s + 1] = o;
         else top = o;
     }
-    if (out && (unsigned)cu.st_rel < (unsigned)rows) *reinterpret_cast<float4 *>(out + cu.st_off) = top;
+    if (out && (unsigned)cu.st_rel < (unsigned)rows) *reinterpret_cast<V *>(out + cu.st_off) = Store<T>::from_f4(top);
     if (PREV && outp && (unsigned)(cu.st_rel + 1) < (unsigned)rows)
-        *reinterpret_cast<float4 *>(outp + cu.st_off + a.ld) = N[L - 1];
+        *reinterpret_cast<V *>(outp + cu.st_off + a.ld) = Store<T>::from_f4(N[L - 1]);
     cu.st_off += a.ld;
     cu.st_rel += 1;
 }
 
-template <int L, bool PREV, int K>
-__device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[L + 1], float4 *pr, float4 *br,
-                                             Cursor &cu, const StreamArgs &a, int nsteps, int rows, float *out,
-                                             float *outp)
+template <typename T, int L, bool PREV, int K>
+__device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[L + 1],
+                                             typename Store<T>::Vec *pr, typename Store<T>::Vec *br, Cursor<T> &cu,
+                                             const StreamArgs<T> &a, int nsteps, int rows, T *out, T *outp)
 {
-    if constexpr (K < Ring<L>::U) {
+    if constexpr (K < Ring<T, L>::U) {
         if (t + K < nsteps) {
-            stream_step<L, PREV, K>(t + K, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
-            stream_steps<L, PREV, K + 1>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_step<T, L, PREV, K>(t + K, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_steps<T, L, PREV, K + 1>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
         }
     }
 }
@@ -172,11 +188,13 @@ __device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&
 template <int L>
 constexpr int min_blocks() { return L >= 7 ? 2 : 3; }
 
-template <int G, int L, bool PREV>
-__global__ void __launch_bounds__(128, min_blocks<L>()) k_sweep_stream(StreamArgs a)
+template <typename T, int G, int L, bool PREV>
+__global__ void __launch_bounds__(128, min_blocks<L>()) k_sweep_stream(StreamArgs<T> a)
 {
     static_assert(L >= 1 && L <= G && G % 4 == 0, "fusion depth must fit the halo");
-    extern __shared__ float4 sm_rings[];
+    using V = typename Store<T>::Vec;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    V *sm_rings = reinterpret_cast<V *>(sm_raw);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int wid = blockIdx.x * 4 + wib;
     if (wid >= a.nwork) return;  // whole warp
@@ -192,18 +210,18 @@ __global__ void __launch_bounds__(128, min_blocks<L>()) k_sweep_stream(StreamArg
     const int ybeg = y0 - L;
     const int nsteps = rows + 2 * L;
 
-    float4 *pr = sm_rings + wib * Ring<L>::floats4_per_warp + lane;
-    float4 *br = pr + kRP * 32;
+    V *pr = sm_rings + wib * Ring<T, L>::vecs_per_warp + lane;
+    V *br = pr + kRP * 32;
 
-    Cursor cu;
+    Cursor<T> cu;
     cu.ld_row = ybeg % a.h;
     if (cu.ld_row < 0) cu.ld_row += a.h;
     cu.gp = a.pin + (size_t)cu.ld_row * a.ld + cx;
     cu.gb = a.b + (size_t)cu.ld_row * a.ld + cx;
     cu.st_rel = -2 * L;  // level L at step 0 is row ybeg - L = y0 - 2L
     cu.st_off = (long long)(y0 - 2 * L) * a.ld;
-    float *out = st_lane ? a.pout + cx : nullptr;
-    float *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
+    T *out = st_lane ? a.pout + cx : nullptr;
+    T *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
 #pragma unroll
     for (int k = 0; k < kRP - 1; ++k) {
         if (k < nsteps) prefetch_row(cu, pr, br, k, a);
@@ -217,31 +235,50 @@ __global__ void __launch_bounds__(128, min_blocks<L>()) k_sweep_stream(StreamArg
 #pragma unroll
     for (int s = 0; s <= L; ++s) bq[s] = z;
 
-    for (int t = 0; t < nsteps; t += Ring<L>::U)
-        stream_steps<L, PREV, 0>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+    for (int t = 0; t < nsteps; t += Ring<T, L>::U)
+        stream_steps<T, L, PREV, 0>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
     cp_async_wait<0>();
 }
 
-template <int G, int L, bool PREV>
-cudaError_t launch_stream_t(const StreamArgs &a, cudaStream_t st)
+template <typename T, int G, int L, bool PREV>
+cudaError_t launch_stream_t(const StreamArgs<T> &a, cudaStream_t st)
 {
-    constexpr int smem = Ring<L>::bytes_per_block;
+    constexpr int smem = Ring<T, L>::bytes_per_block;
     static bool attr_set = false;  // per instantiation; the attribute is per function
     if (!attr_set) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_sweep_stream<G, L, PREV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        const cudaError_t e = cudaFuncSetAttribute(k_sweep_stream<T, G, L, PREV>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     const int blocks = (a.nwork + 3) / 4;  // 4 warps per block: the shared rings are laid out for 4
-    k_sweep_stream<G, L, PREV><<<blocks, 128, smem, st>>>(a);
+    k_sweep_stream<T, G, L, PREV><<<blocks, 128, smem, st>>>(a);
     return launched();
 }
 
-template <int G, int L>
-cudaError_t launch_stream_l(const StreamArgs &a, bool prev, cudaStream_t st)
+template <typename T, int G, int L>
+cudaError_t launch_stream_l(const StreamArgs<T> &a, bool prev, cudaStream_t st)
 {
-    return prev ? launch_stream_t<G, L, true>(a, st) : launch_stream_t<G, L, false>(a, st);
+    return prev ? launch_stream_t<T, G, L, true>(a, st) : launch_stream_t<T, G, L, false>(a, st);
+}
+
+template <typename T>
+StreamArgs<T> stream_args(const T *pin, const T *b, T *pout, T *pprev, int ld, int w, int h, int halo, int chunk,
+                          const int *done)
+{
+    StreamArgs<T> a;
+    a.pin = pin;
+    a.b = b;
+    a.pout = pout;
+    a.pprev = pprev;
+    a.done = done;
+    a.ld = ld;
+    a.w = w;
+    a.h = h;
+    a.chunk = chunk;
+    a.nsx = (w + 128 - 2 * halo - 1) / (128 - 2 * halo);
+    a.nwork = a.nsx * ((h + chunk - 1) / chunk);
+    return a;
 }
 
 }  // namespace
@@ -261,42 +298,64 @@ cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, i
 cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
                                 int h, int levels, int halo, int chunk, const int *done, cudaStream_t st)
 {
-    StreamArgs a;
-    a.done = done;
-    a.pin = pin;
-    a.b = b;
-    a.pout = pout;
-    a.pprev = pprev;
-    a.ld = ld;
-    a.w = w;
-    a.h = h;
-    a.chunk = chunk;
-    a.nsx = (w + stream_strip_width(halo) - 1) / stream_strip_width(halo);
-    a.nwork = a.nsx * ((h + chunk - 1) / chunk);
+    const StreamArgs<float> a = stream_args(pin, b, pout, pprev, ld, w, h, halo, chunk, done);
     const bool prev = pprev != nullptr;
     if (halo == 4) {
         switch (levels) {
-        case 1: return launch_stream_l<4, 1>(a, prev, st);
-        case 2: return launch_stream_l<4, 2>(a, prev, st);
-        case 3: return launch_stream_l<4, 3>(a, prev, st);
-        case 4: return launch_stream_l<4, 4>(a, prev, st);
+        case 1: return launch_stream_l<float, 4, 1>(a, prev, st);
+        case 2: return launch_stream_l<float, 4, 2>(a, prev, st);
+        case 3: return launch_stream_l<float, 4, 3>(a, prev, st);
+        case 4: return launch_stream_l<float, 4, 4>(a, prev, st);
         default: return cudaErrorInvalidValue;
         }
     }
     if (halo == 8) {
         switch (levels) {
-        case 1: return launch_stream_l<8, 1>(a, prev, st);
-        case 2: return launch_stream_l<8, 2>(a, prev, st);
-        case 3: return launch_stream_l<8, 3>(a, prev, st);
-        case 4: return launch_stream_l<8, 4>(a, prev, st);
-        case 5: return launch_stream_l<8, 5>(a, prev, st);
-        case 6: return launch_stream_l<8, 6>(a, prev, st);
-        case 7: return launch_stream_l<8, 7>(a, prev, st);
-        case 8: return launch_stream_l<8, 8>(a, prev, st);
+        case 1: return launch_stream_l<float, 8, 1>(a, prev, st);
+        case 2: return launch_stream_l<float, 8, 2>(a, prev, st);
+        case 3: return launch_stream_l<float, 8, 3>(a, prev, st);
+        case 4: return launch_stream_l<float, 8, 4>(a, prev, st);
+        case 5: return launch_stream_l<float, 8, 5>(a, prev, st);
+        case 6: return launch_stream_l<float, 8, 6>(a, prev, st);
+        case 7: return launch_stream_l<float, 8, 7>(a, prev, st);
+        case 8: return launch_stream_l<float, 8, 8>(a, prev, st);
         default: return cudaErrorInvalidValue;
         }
     }
     return cudaErrorInvalidValue;
+}
+
+// 16-bit storage (halo 8, levels 1..8, no second-to-last output): the
+// iterate and the right-hand side are stored bf16 / fp16 and every sweep is
+// computed in FP32 between the load of the input and the store of the output.
+template <typename T>
+static cudaError_t launch_sweep_stream_lp(const T *pin, const T *b, T *pout, int ld, int w, int h, int levels,
+                                          int chunk, cudaStream_t st)
+{
+    const StreamArgs<T> a = stream_args<T>(pin, b, pout, nullptr, ld, w, h, 8, chunk, nullptr);
+    switch (levels) {
+    case 1: return launch_stream_t<T, 8, 1, false>(a, st);
+    case 2: return launch_stream_t<T, 8, 2, false>(a, st);
+    case 3: return launch_stream_t<T, 8, 3, false>(a, st);
+    case 4: return launch_stream_t<T, 8, 4, false>(a, st);
+    case 5: return launch_stream_t<T, 8, 5, false>(a, st);
+    case 6: return launch_stream_t<T, 8, 6, false>(a, st);
+    case 7: return launch_stream_t<T, 8, 7, false>(a, st);
+    case 8: return launch_stream_t<T, 8, 8, false>(a, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_sweep_stream_bf16(const __nv_bfloat16 *pin, const __nv_bfloat16 *b, __nv_bfloat16 *pout, int ld,
+                                     int w, int h, int levels, int chunk, cudaStream_t st)
+{
+    return launch_sweep_stream_lp(pin, b, pout, ld, w, h, levels, chunk, st);
+}
+
+cudaError_t launch_sweep_stream_f16(const __half *pin, const __half *b, __half *pout, int ld, int w, int h,
+                                    int levels, int chunk, cudaStream_t st)
+{
+    return launch_sweep_stream_lp(pin, b, pout, ld, w, h, levels, chunk, st);
 }
 
 }  // namespace pfs

@@ -30,6 +30,8 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libpfs_gb300.so")
 
 PFS_HOST, PFS_DEVICE = 0, 1
+PREC_F32, PREC_BF16, PREC_F16, PREC_F64 = 0, 1, 2, 3
+PRECISIONS = {"f32": PREC_F32, "bf16": PREC_BF16, "f16": PREC_F16, "f64": PREC_F64}
 
 
 class PFSError(RuntimeError):
@@ -46,7 +48,7 @@ class Params(C.Structure):
     """pfs_params (include/pfs.h)."""
     _fields_ = [("dt", C.c_float), ("viscosity", C.c_float), ("diffuse_iters", C.c_int), ("max_iters", C.c_int),
                 ("tol", C.c_double), ("check_every", C.c_int), ("fuse_depth", C.c_int), ("chunk_rows", C.c_int),
-                ("want_residual", C.c_int)]
+                ("want_residual", C.c_int), ("precision", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -85,6 +87,7 @@ SIGNATURES = [
     ("pfs_session_upload", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("pfs_session_step", C.c_int, [C.c_void_p, C.c_int]),
     ("pfs_session_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    ("pfs_session_download_f64", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("pfs_session_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("pfs_session_sync", C.c_int, [C.c_void_p]),
     ("pfs_session_destroy", C.c_int, [C.c_void_p]),
@@ -235,6 +238,22 @@ class Session:
                                           C.c_void_p(_ptr(tmp) if tmp is not None else None),
                                           C.c_void_p(_ptr(image) if image is not None else None), where))
         return vp, tmp, image
+
+    def download_f64(self, vp=None, image=None):
+        """The state in float64 (numpy float64 arrays -> host): vp (u, v, p, b), image."""
+        ref = vp if vp is not None else image
+        where = PFS_HOST if isinstance(ref, np.ndarray) else PFS_DEVICE
+
+        def addr(a):
+            if a is None:
+                return None
+            if isinstance(a, np.ndarray):
+                if a.dtype != np.float64 or not a.flags.c_contiguous:
+                    raise ValueError("float64 C-contiguous arrays expected")
+                return a.ctypes.data
+            return a.data_ptr()
+        _check(lib().pfs_session_download_f64(self._h, C.c_void_p(addr(vp)), C.c_void_p(addr(image)), where))
+        return vp, image
 
     def stats(self) -> dict:
         s = Stats()
