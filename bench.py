@@ -68,6 +68,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-budget-s", type=float, default=90.0)
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision / batched form measurements")
+    ap.add_argument("--form-size", type=int, default=4096)
+    ap.add_argument("--form-steps", type=int, default=5)
+    ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--ens-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -215,6 +220,126 @@ def reference_arm(a, rank):
 
 
 # ---------------------------------------------------------------------------------------------
+# The other forms (precision, batched), each against the plain FP32 path on the same workload
+
+def time_session(fluid, vp, tmp, img, steps, stream, **kw):
+    import torch
+    h, w, _ = vp.shape
+    with fluid.Session(w, h, image_shape=img.shape, stream=stream, **kw) as s:
+        s.upload(vp, tmp, img)
+        s.step(1)
+        s.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            s.step(1)
+        e1.record()
+        torch.cuda.synchronize()
+        st = s.stats()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": w * h / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "sweeps_per_step": st["sweeps"],
+            "final_rel_residual": st["rel_residual"]}
+
+
+def precision_forms(a, fluid, synthetic, stream):
+    n = a.form_size
+    vp, tmp, img, _ = synthetic.initial_state(n, n, a.channels, a.seed)
+    kw = dict(dt=a.dt, diffuse_iters=a.diffuse_iters, max_iters=a.cap, tol=a.tol, check_every=a.check_every)
+    out = {"workload": f"{n}x{n}, same solver settings as the headline, {a.form_steps} steps"}
+    for name, prec in (("plain_f32", fluid.PREC_F32), ("bf16", fluid.PREC_BF16), ("f16", fluid.PREC_F16)):
+        out[name] = time_session(fluid, vp, tmp, img, a.form_steps, stream, precision=prec, **kw)
+    return out
+
+
+def ensemble_sizes(n, seed):
+    from probabilistic_fluid_simulation_gb300 import synthetic
+    rng = synthetic.SplitMix64(seed * 7919 + 17)
+    sides = (64, 128, 256, 512, 1024)
+    return [(sides[int(rng.uniform() * 5)], sides[int(rng.uniform() * 5)]) for _ in range(n)]
+
+
+def ensemble_member(k, w, h, base, channels, seed):
+    from probabilistic_fluid_simulation_gb300 import synthetic as S
+    vort = [S.Vortex(v.cx * w / 1024, v.cy * h / 1024, v.radius * (w * h) ** 0.5 / 1024, v.circulation)
+            for v in S.perturb_vortices(base, seed=seed, member=k)]
+    vp = S.velocity_from_vortices(w, h, vort)
+    return vp, np.zeros_like(vp), S.blob_image(w, h, channels, seed=seed * 1000 + k)
+
+
+def batched_form(a, fluid, synthetic, stream):
+    import torch
+    from probabilistic_fluid_simulation_gb300 import tune
+    sizes = ensemble_sizes(a.members, a.seed)
+    base = synthetic.draw_vortices(1024, 1024, seed=a.seed)
+    states = [ensemble_member(k, w, h, base, a.channels, a.seed) for k, (w, h) in enumerate(sizes)]
+    cells = sum(w * h for w, h in sizes)
+    # the ensemble's sweep cap and check interval must be multiples of the fuse depth: 2000 and 200
+    every = a.check_every if a.check_every % 8 == 0 else 200
+    kw = dict(dt=a.dt, diffuse_iters=a.diffuse_iters, max_iters=a.cap, tol=a.tol, check_every=every)
+    out = {"workload": f"{a.members} members, sides uniform in {{64..1024}} (w, h drawn independently), "
+                       f"{cells} cells, perturbed vortex fields (+N(0,0.05) circulation, +N(0,2) cells), "
+                       f"residual {a.tol:g} checked every {every} sweeps, cap {a.cap}"}
+    with fluid.Ensemble(sizes, a.channels, stream=stream, **kw) as ens:
+        for k, st in enumerate(states):
+            ens.upload(k, *st)
+        best, timings = tune.tune_ensemble(ens, steps=1)
+        ens.step(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = fluid.kernel_launches()
+        e0.record()
+        ens.step(a.ens_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / a.ens_steps
+        launches = (fluid.kernel_launches() - l0) / a.ens_steps
+        info = ens.info()
+        stats = [ens.stats(k) for k in range(len(sizes))]
+        sample = [0, len(sizes) // 3, 2 * len(sizes) // 3, len(sizes) - 1]
+        ens_out = {}
+        for k in sample:
+            vpo, imo = np.empty_like(states[k][0]), np.empty_like(states[k][2])
+            ens.download(k, vpo, imo)
+            ens_out[k] = (vpo, imo)
+    out["batched"] = {"value": cells / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": a.ens_steps,
+                      "launches_per_step": launches, "graph": bool(info["graphs"]), "grid_blocks": info["grid_blocks"],
+                      "autotuned": {"fuse_depth": best[0], "chunk_rows": best[1],
+                                    "candidates_ms": [[f, c, round(t, 3)] for f, c, t in timings]},
+                      "mean_sweeps": float(np.mean([s["sweeps"] for s in stats])),
+                      "capped": int(sum(s["capped"] for s in stats))}
+    # the sampled members through plain sessions with the same steps (the tuner restores the
+    # initial state, then 1 + ens_steps steps ran): fields must be identical
+    maxdiff = 0.0
+    for k in sample:
+        vp, tmp, img = states[k]
+        h, w, _ = vp.shape
+        with fluid.Session(w, h, image_shape=img.shape, stream=stream, **kw) as s:
+            s.upload(vp, tmp, img)
+            s.step(1 + a.ens_steps)
+            vpo, imo = np.empty_like(vp), np.empty_like(img)
+            s.download(vpo, None, imo)
+        ev, ei = ens_out[k]
+        maxdiff = max(maxdiff, float(np.abs(ev[..., :2] - vpo[..., :2]).max()), float(np.abs(ei - imo).max()))
+    # plain-session throughput on the whole ensemble: one step of every member
+    sess = []
+    for k, (vp, tmp, img) in enumerate(states):
+        h, w, _ = vp.shape
+        s = fluid.Session(w, h, image_shape=img.shape, stream=stream, **kw)
+        s.upload(vp, tmp, img)
+        sess.append(s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in sess:
+        s.step(1)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    for s in sess:
+        s.close()
+    out["plain_sessions"] = {"value": cells / el, "unit": UNIT, "ms_per_step": el * 1e3,
+                             "how": "one pfs_session per member, stepped one after another (1 step each)"}
+    out["members_checked_vs_sessions"] = {"members": sample, "max_abs_diff": maxdiff}
+    return out
+
 
 def main():
     a = parse()
@@ -334,6 +459,11 @@ def main():
                "api": "pfs_session_upload(PFS_HOST) + pfs_session_step(1) + pfs_session_download(PFS_HOST)"}
     sess.close()
 
+    forms = None
+    if rank == 0 and not a.no_forms:
+        forms = {"precision": precision_forms(a, fluid, synthetic, stream),
+                 "batched": batched_form(a, fluid, synthetic, stream)}
+
     cpu = None
     if rank == 0 and not a.no_cpu and a.cpu_steps > 0:
         val, done, el, threads, cs = cpu_run(a, a.cpu_steps)
@@ -348,7 +478,7 @@ def main():
                 "vs_baseline": None, "dtype": "f32", "data": DATA,
                 "config": config(a, {"fuse_depth": levels, "chunk_rows": chunk}),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk,
+                "clocks": clk, "forms": forms,
                 "solver": {"sweeps_per_step": mean_sweeps, "cap_hits": st1["cap_hits"] - st0["cap_hits"],
                            "final_rel_residual": st1["rel_residual"],
                            "cell_sweeps_per_s": cells * mean_sweeps * a.steps * world / (ms / 1e3)}}

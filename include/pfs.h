@@ -194,6 +194,34 @@ int pfs_session_stats(pfs_session *s, pfs_stats *out);
 int pfs_session_sync(pfs_session *s);
 int pfs_session_destroy(pfs_session *s);
 
+/* ---- ensembles: many independent simulations in one persistent kernel ------------ */
+/*
+ * n members with their own grid sizes (widths multiples of 4) and a common
+ * image channel count, advanced together: each timestep of all members is one
+ * cooperative launch (replayed from a CUDA graph where the driver accepts the
+ * capture) that walks advection, divergence, phases of fused sweeps, residual
+ * checks and projection + image advection with grid-wide barriers between
+ * phases; members that converge stop taking sweep work. Each member's fields
+ * are bit-identical to a session with the same parameters. Float32, viscosity
+ * 0, even diffusion count; max_iters and check_every multiples of the fuse
+ * depth (4 or 8). No counterpart in the reference, which runs one simulation.
+ */
+typedef struct pfs_ensemble pfs_ensemble;
+int pfs_ensemble_create(pfs_ensemble **out, int n, const int *vx, const int *vy, int channels,
+                        const pfs_params *params, void *stream);
+/* member k's state in the reference layout (vp, tmp: (vy, vx, 4); image (vy, vx, channels)) */
+int pfs_ensemble_upload(pfs_ensemble *e, int k, const float *vp, const float *tmp, const float *image, int where);
+int pfs_ensemble_step(pfs_ensemble *e, int steps);
+/* member k: vp = (u, v, final pressure, divergence) and the image */
+int pfs_ensemble_download(pfs_ensemble *e, int k, float *vp, float *image, int where);
+int pfs_ensemble_member_stats(pfs_ensemble *e, int k, pfs_stats *out);
+/* tile configuration of the sweep phases (the autotuner's knobs) */
+int pfs_ensemble_config(pfs_ensemble *e, int fuse_depth, int chunk_rows);
+int pfs_ensemble_info(pfs_ensemble *e, int *fuse_depth, int *chunk_rows, int *grid_blocks, int *graphs);
+/* restore == 0: copy the whole state aside (device to device); 1: put it back */
+int pfs_ensemble_snapshot(pfs_ensemble *e, int restore);
+int pfs_ensemble_destroy(pfs_ensemble *e);
+
 /* ---- kernel-level entry points (tests, tuning, benchmarks) ------------------------ */
 /*
  * `levels` pressure Jacobi sweeps (src/fluid.cpp:239-257) on planar fields:

@@ -40,6 +40,7 @@ cudaStream_t g_stream = nullptr;
 
 int fail(int code, const char *fmt, ...)
 {
+    if (code == PFS_ERR_CUDA) cudaGetLastError();  // reported through the status; clear the non-sticky error
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -53,6 +54,7 @@ int fail(int code, const char *fmt, ...)
 
 int pfs::record_error(int code, const char *msg)
 {
+    if (code == PFS_ERR_CUDA) cudaGetLastError();  // reported through the status; clear the non-sticky error
     g_err = msg;
     return code;
 }

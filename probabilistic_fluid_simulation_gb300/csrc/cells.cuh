@@ -1,0 +1,165 @@
+// Per-cell pieces of the timestep (advection, divergence, projection, image
+// advection, exact residual) shared by the step kernels (step_kernels.cu) and
+// the persistent ensemble kernel (ensemble.cu). Every formula keeps the
+// reference's operation order (src/fluid.cpp, cited per function).
+#pragma once
+
+#include "common.cuh"
+#include "reduce.cuh"
+
+namespace pfs {
+namespace {
+
+__device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__device__ __forceinline__ int wp(int i, int n) { return i + 1 == n ? 0 : i + 1; }
+
+// Backtrace, wrap and corner cells of one sample (src/fluid.cpp:39-58 and
+// :97-114): x' = i - (k*u)/n wrapped to [0, n).
+struct Corners {
+    int i0, i1, j0, j1;
+    float sx, sy;
+};
+
+__device__ __forceinline__ Corners backtrace(int i, int j, float kx, float ky, float u, float v, float fw, float fh,
+                                            int w, int h)
+{
+    float xp = fsub((float)i, fdiv(fmul(kx, u), fw));
+    float yp = fsub((float)j, fdiv(fmul(ky, v), fh));
+    xp = wrap_coord(xp, fw);
+    yp = wrap_coord(yp, fh);
+    Corners c;
+    c.i0 = cell_of(xp, w);
+    c.j0 = cell_of(yp, h);
+    c.i1 = (c.i0 + 1) % w;
+    c.j1 = (c.j0 + 1) % h;
+    c.sx = fsub(xp, (float)c.i0);
+    c.sy = fsub(yp, (float)c.j0);
+    return c;
+}
+
+// Velocity advection of cell (i, j), src/fluid.cpp:24-70.
+__device__ __forceinline__ void advect_cell(const float *__restrict__ u, const float *__restrict__ v,
+                                            float *__restrict__ uo, float *__restrict__ vo, int ld, int w, int h,
+                                            float dt, int i, int j)
+{
+    const size_t o = (size_t)j * ld + i;
+    const Corners c = backtrace(i, j, dt, dt, u[o], v[o], (float)w, (float)h, w, h);
+    const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
+    uo[o] = bilerp(c.sx, c.sy, u[r0 + c.i0], u[r0 + c.i1], u[r1 + c.i0], u[r1 + c.i1]);
+    vo[o] = bilerp(c.sx, c.sy, v[r0 + c.i0], v[r0 + c.i1], v[r1 + c.i0], v[r1 + c.i1]);
+}
+
+// Divergence of cell (i, j) into b, src/fluid.cpp:218-237; returns it.
+__device__ __forceinline__ float divergence_cell(const float *__restrict__ u, const float *__restrict__ v,
+                                                 float *__restrict__ b, int ld, int w, int h, float gamma, int i,
+                                                 int j)
+{
+    const size_t r = (size_t)j * ld;
+    const float du = fsub(u[r + wp(i, w)], u[r + wm(i, w)]);
+    const float dv = fsub(v[(size_t)wp(j, h) * ld + i], v[(size_t)wm(j, h) * ld + i]);
+    const float bv = fmul(gamma, fadd(du, dv));
+    b[r + i] = bv;
+    return bv;
+}
+
+// Residual of the pressure system (src/fluid.cpp:239-257 solves 4p - sum nb = b),
+// r = b + pL + pR + pT + pB - 4p. The five additions are error-free (TwoSum),
+// so hi + lo carries r with a relative error near 2^-48 (the error terms are
+// summed in float). r^2 = hi^2 + (fma error of hi^2) + 2 hi lo is added to
+// the float-float accumulator.
+__device__ __forceinline__ void residual_sq(FFAcc &acc, float b, float l, float r, float t, float bo, float c)
+{
+    FF s = two_sum(b, l);
+    float e = s.lo;
+    s = two_sum(s.hi, r);
+    e = __fadd_rn(e, s.lo);
+    s = two_sum(s.hi, t);
+    e = __fadd_rn(e, s.lo);
+    s = two_sum(s.hi, bo);
+    e = __fadd_rn(e, s.lo);
+    s = two_sum(s.hi, __fmul_rn(-4.0f, c));  // -4p is exact
+    e = __fadd_rn(e, s.lo);
+    const FF q = two_sum(s.hi, e);
+    const float sq = __fmul_rn(q.hi, q.hi);
+    const float sq_err = __fmaf_rn(q.hi, q.hi, -sq);
+    const float cross = __fmul_rn(__fmul_rn(2.0f, q.hi), q.lo);
+    acc.add(sq, __fadd_rn(sq_err, cross));
+}
+
+// Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2.
+__device__ __forceinline__ void project_cell(const float *__restrict__ u, const float *__restrict__ v,
+                                             const float *__restrict__ p, int ld, int w, int h, float dt, int i,
+                                             int j, float &uo, float &vo)
+{
+    const size_t r = (size_t)j * ld;
+    const float gx = fmul(fmul(fsub(p[r + wp(i, w)], p[r + wm(i, w)]), dt), 0.5f);
+    const float gy = fmul(fmul(fsub(p[(size_t)wp(j, h) * ld + i], p[(size_t)wm(j, h) * ld + i]), dt), 0.5f);
+    uo = fsub(u[r + i], gx);
+    vo = fsub(v[r + i], gy);
+}
+
+// Projection then image advection of cell (i, j) with the just-projected
+// velocity (image grid = velocity grid: viw = vih = 1, and dt / viw = dt).
+__device__ __forceinline__ void project_image_cell(const float *__restrict__ u, const float *__restrict__ v,
+                                                   const float *__restrict__ p, float *__restrict__ uo,
+                                                   float *__restrict__ vo, int ld, int w, int h, float dt,
+                                                   const float *__restrict__ img, float *__restrict__ imgo,
+                                                   size_t plane, int c, int i, int j)
+{
+    float un, vn;
+    project_cell(u, v, p, ld, w, h, dt, i, j, un, vn);
+    const size_t o = (size_t)j * ld + i;
+    uo[o] = un;
+    vo[o] = vn;
+    const Corners k = backtrace(i, j, dt, dt, un, vn, (float)w, (float)h, w, h);
+    const size_t r0 = (size_t)k.j0 * ld, r1 = (size_t)k.j1 * ld;
+    for (int ch = 0; ch < c; ++ch) {
+        const float *s = img + ch * plane;
+        imgo[ch * plane + o] = bilerp(k.sx, k.sy, s[r0 + k.i0], s[r0 + k.i1], s[r1 + k.i0], s[r1 + k.i1]);
+    }
+}
+
+// Residual sums of one warp task of the strip residual: strip sx (128
+// columns, four per lane), rows [y0, y1). Adds r^2 into acc[0..3] (one chain
+// per lane column) and, with accb, b^2.
+__device__ __forceinline__ void residual_strip_task(const float *__restrict__ p, const float *__restrict__ b, int ld,
+                                                    int w, int h, int sx, int y0, int y1, int lane, FFAcc (&acc)[4],
+                                                    FFAcc *accb)
+{
+    const int x = sx * 128 + 4 * lane;
+    const bool active = x < w;
+    const int xs = active ? x : w - 4;  // inactive lanes shadow a valid column, results discarded
+    const int last_lane = min(31, (w - sx * 128) / 4 - 1);
+    const int xl = (sx * 128 == 0) ? w - 1 : sx * 128 - 1;  // left outside neighbour
+    const int xr = (sx * 128 + 4 * (last_lane + 1)) % w;    // right outside neighbour
+    // loads bypass L1 (ld.global.cg): inside the persistent ensemble kernel the
+    // pressure planes are rewritten by other blocks between checks
+    const float *pc = p + xs;
+    float4 up = __ldcg(reinterpret_cast<const float4 *>(pc + (size_t)wm(y0, h) * ld));
+    float4 cu = __ldcg(reinterpret_cast<const float4 *>(pc + (size_t)y0 * ld));
+    for (int y = y0; y < y1; ++y) {
+        const float4 dn = __ldcg(reinterpret_cast<const float4 *>(pc + (size_t)wp(y, h) * ld));
+        const float4 bb = __ldcg(reinterpret_cast<const float4 *>(b + (size_t)y * ld + xs));
+        float lft = __shfl_up_sync(0xffffffffu, cu.w, 1);
+        float rgt = __shfl_down_sync(0xffffffffu, cu.x, 1);
+        if (lane == 0) lft = __ldcg(p + (size_t)y * ld + xl);
+        if (lane == last_lane) rgt = __ldcg(p + (size_t)y * ld + xr);
+        if (active) {
+            residual_sq(acc[0], bb.x, lft, cu.y, up.x, dn.x, cu.x);
+            residual_sq(acc[1], bb.y, cu.x, cu.z, up.y, dn.y, cu.y);
+            residual_sq(acc[2], bb.z, cu.y, cu.w, up.z, dn.z, cu.z);
+            residual_sq(acc[3], bb.w, cu.z, rgt, up.w, dn.w, cu.w);
+            if (accb) {
+                acc_square(*accb, bb.x);
+                acc_square(*accb, bb.y);
+                acc_square(*accb, bb.z);
+                acc_square(*accb, bb.w);
+            }
+        }
+        up = cu;
+        cu = dn;
+    }
+}
+
+}  // namespace
+}  // namespace pfs

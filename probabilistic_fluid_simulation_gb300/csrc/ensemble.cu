@@ -1,0 +1,723 @@
+// Batched form: an ensemble of independent simulations of uneven grid sizes
+// advanced together, one persistent cooperative kernel per timestep.
+//
+// Each member runs the plain float32 step with viscosity 0 and an even
+// diffusion count (where the reference's buffer roles reduce to: advect;
+// divergence of the advected velocity; Jacobi from the previous final
+// pressure; projection with the final pressure; image advection), with the
+// same per-cell arithmetic as the single-simulation kernels (cells.cuh,
+// sweep_stream.cuh), so every member's fields are bit-identical to a plain
+// session's.
+//
+// The kernel walks the phases of the step (advect, divergence, fused sweep
+// phases of L sweeps, residual checks, projection + image) with a grid
+// barrier between phases. A phase is a task list over all members (row tasks,
+// sweep strips x chunks, residual strips): warps take tasks in stride, and a
+// member that has converged contributes no tasks to later sweep phases. All
+// active members advance in lockstep, so the pressure plane a phase reads is
+// (start plane + phase index) mod 2 for every member, and no per-member
+// barrier is needed.
+//
+// The grid barrier spins with an iteration limit: on timeout it raises an
+// error flag and every block returns, so a fault cannot hang the device.
+// Cooperative launch guarantees all blocks are resident.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cells.cuh"
+#include "kernels.h"
+#include "pfs.h"
+#include "reduce.cuh"
+#include "sweep_stream.cuh"
+
+namespace pfs {
+namespace {
+
+struct Member {
+    int w, h, ld;
+    float *u[2], *v[2];  // [0] current velocity, [1] advected
+    float *p[2];         // pressure ping-pong
+    float *b;
+    float *img[2];       // image ping-pong, c planes of ld*h each
+    int row_task0, nrow;     // row tasks (8 rows): advect, divergence, projection + image
+    int sw_task0, nsx, nsy;  // fused sweep tasks
+    int rs_task0, rsx, rsy;  // residual strip tasks
+};
+
+struct MemberState {
+    int cur;      // plane holding the pressure iterate at the start of the step (the final one after it)
+    int done;     // pressure solve finished this step
+    int sweeps;   // sweeps of this step
+    int checks;   // residual evaluations of this step
+    int capped;
+    int pad;
+    double rel;   // last relative residual
+    double bb;    // sum b^2
+};
+
+struct EnsArgs {
+    const Member *mem;
+    MemberState *state;
+    int nmem;
+    const int *row_member, *sw_member, *rs_member;  // task -> member
+    int nrow_tasks, nsw_tasks, nrs_tasks;
+    double *row_part, *rs_part;  // per-task partial sums
+    unsigned *bar_count, *bar_gen;
+    int *err;
+    int *active;  // members still iterating, one counter per check
+    float dt, gamma;
+    double tol;
+    int cap, check_every, chunk, channels, icur;
+};
+
+constexpr int kRowsPerTask = 8;
+constexpr long long kBarrierSpinLimit = 1LL << 24;  // ~1-2 s with the back-off below
+
+// Grid-wide barrier with a bounded wait. Returns false (and every later call
+// returns false at once) if any block gave up waiting.
+__device__ bool grid_sync(const EnsArgs &a)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned *gen = a.bar_gen;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(a.bar_count, 1u) == gridDim.x - 1) {
+            *a.bar_count = 0u;
+            __threadfence();
+            atomicAdd(a.bar_gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*gen == g) {
+                if (*(volatile int *)a.err || ++spins > kBarrierSpinLimit) {
+                    atomicExch(a.err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (*(volatile int *)a.err) ok = 0;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Member state and per-task partials are written by one block and read by
+// others later in the same launch: read them around L1 (which is not
+// coherent across SMs).
+template <typename T>
+__device__ __forceinline__ T vload(const T &x) { return *(const volatile T *)&x; }
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int G, int L>
+__global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
+{
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    using V = Store<float>::Vec;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * 4 + wib, nw = gridDim.x * 4;
+    V *ring = reinterpret_cast<V *>(sm_raw) + wib * Ring<float, L>::vecs_per_warp;
+    const int ic = a.icur, io = 1 - a.icur;
+
+    // advect every member: u[0], v[0] -> u[1], v[1]
+    for (int t = gw; t < a.nrow_tasks; t += nw) {
+        const Member &m = a.mem[a.row_member[t]];
+        const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+        for (int j = r0; j < r1; ++j)
+            for (int i = lane; i < m.w; i += 32) advect_cell(m.u[0], m.v[0], m.u[1], m.v[1], m.ld, m.w, m.h, a.dt, i, j);
+    }
+    if (!grid_sync(a)) return;
+
+    // divergence of the advected velocity, b^2 per task
+    for (int t = gw; t < a.nrow_tasks; t += nw) {
+        const Member &m = a.mem[a.row_member[t]];
+        const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+        FFAcc acc;
+        for (int j = r0; j < r1; ++j)
+            for (int i = lane; i < m.w; i += 32)
+                acc_square(acc, divergence_cell(m.u[1], m.v[1], m.b, m.ld, m.w, m.h, a.gamma, i, j));
+        const double s = warp_sum(acc.value());
+        if (lane == 0) a.row_part[t] = s;
+    }
+    if (!grid_sync(a)) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+        const Member &m = a.mem[k];
+        double s = 0.0;
+        for (int t = 0; t < m.nrow; ++t) s += __ldcg(a.row_part + m.row_task0 + t);
+        volatile MemberState &ms = a.state[k];
+        ms.bb = s;
+        ms.done = 0;
+        ms.sweeps = 0;
+        ms.checks = 0;
+        ms.capped = 0;
+    }
+    if (!grid_sync(a)) return;
+
+    // pressure: phases of L fused sweeps; residual checks every check_every sweeps and at the cap
+    int phase = 0, check = 0;
+    for (int s = 0; s < a.cap;) {
+        for (int t = gw; t < a.nsw_tasks; t += nw) {
+            const int mi = a.sw_member[t];
+            if (vload(a.state[mi].done)) continue;
+            const int cur = vload(a.state[mi].cur);
+            const Member &m = a.mem[mi];
+            StreamArgs<float> sa;
+            sa.pin = m.p[(cur + phase) & 1];
+            sa.pout = m.p[(cur + phase + 1) & 1];
+            sa.b = m.b;
+            sa.pprev = nullptr;
+            sa.done = nullptr;
+            sa.ld = m.ld;
+            sa.w = m.w;
+            sa.h = m.h;
+            sa.nsx = m.nsx;
+            sa.nwork = m.nsx * m.nsy;
+            sa.chunk = a.chunk;
+            stream_task<float, G, L, false>(sa, t - m.sw_task0, lane, ring);
+        }
+        ++phase;
+        s += L;
+        if (!grid_sync(a)) return;
+        if (s % a.check_every != 0 && s != a.cap) continue;
+        for (int t = gw; t < a.nrs_tasks; t += nw) {
+            const int mi = a.rs_member[t];
+            if (vload(a.state[mi].done)) continue;
+            const int cur = vload(a.state[mi].cur);
+            const Member &m = a.mem[mi];
+            const int q = t - m.rs_task0, sx = q % m.rsx, sy = q / m.rsx;
+            const int y0 = sy * 8, y1 = min(m.h, y0 + 8);
+            FFAcc acc[4];
+            residual_strip_task(m.p[(cur + phase) & 1], m.b, m.ld, m.w, m.h, sx, y0, y1, lane, acc, nullptr);
+            const double v = warp_sum((acc[0].value() + acc[1].value()) + (acc[2].value() + acc[3].value()));
+            if (lane == 0) a.rs_part[t] = v;
+        }
+        if (!grid_sync(a)) return;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+            volatile MemberState &ms = a.state[k];
+            if (ms.done) continue;
+            const Member &m = a.mem[k];
+            double rr = 0.0;
+            for (int t = 0; t < m.rsx * m.rsy; ++t) rr += __ldcg(a.rs_part + m.rs_task0 + t);
+            const double bb = ms.bb;
+            const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
+            ms.rel = rel;
+            ms.checks = ms.checks + 1;
+            if (rel <= a.tol || s == a.cap) {
+                ms.done = 1;
+                ms.sweeps = s;
+                ms.capped = (a.tol > 0.0 && rel > a.tol) ? 1 : 0;
+                ms.cur = (ms.cur + phase) & 1;
+            } else {
+                atomicAdd(a.active + check, 1);
+            }
+        }
+        if (!grid_sync(a)) return;
+        if (*(volatile int *)(a.active + check) == 0) break;
+        ++check;
+    }
+
+    // projection with the final pressure, then image advection
+    for (int t = gw; t < a.nrow_tasks; t += nw) {
+        const int mi = a.row_member[t];
+        const Member &m = a.mem[mi];
+        const float *pf = m.p[vload(a.state[mi].cur)];
+        const size_t plane = (size_t)m.ld * m.h;
+        const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+        for (int j = r0; j < r1; ++j)
+            for (int i = lane; i < m.w; i += 32)
+                project_image_cell(m.u[1], m.v[1], pf, m.u[0], m.v[0], m.ld, m.w, m.h, a.dt, m.img[ic], m.img[io],
+                                   plane, a.channels, i, j);
+    }
+}
+
+}  // namespace
+
+// =============================================================================================
+// Host side
+
+struct Ensemble {
+    int n = 0, c = 0;
+    pfs_params prm{};
+    cudaStream_t st = nullptr;
+    std::vector<int> w, h, ld;
+    std::vector<size_t> off;  // float offset of each member's planes
+    float *mem = nullptr;
+    size_t floats = 0;
+    Member *dmem = nullptr;
+    MemberState *dstate = nullptr;
+    int *dtasks = nullptr;
+    double *dparts = nullptr;
+    unsigned *dbar = nullptr;  // count, gen
+    int *derr = nullptr, *dactive = nullptr;
+    std::vector<Member> hmem;
+    int nrow = 0, nsw = 0, nrs = 0;
+    int halo = 8, levels = 8, chunk = 32;
+    int grid = 0;
+    int icur = 0;
+    long long steps = 0, total_sweeps = 0, cap_hits = 0;
+    float *stage = nullptr;
+    size_t stage_bytes = 0;
+    float *snap = nullptr;  // state copy for pfs_ensemble_snapshot
+    MemberState *snap_state = nullptr;
+    int snap_icur = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool graphs_ok = true;
+};
+
+namespace {
+
+int ens_fail(int code, const char *msg)
+{
+    cudaGetLastError();  // the status carries the error; do not leave it pending for the caller's next CUDA call
+    return record_error(code, msg);
+}
+
+#define ECK(x)                                                                 \
+    do {                                                                       \
+        cudaError_t e_ = (x);                                                  \
+        if (e_ != cudaSuccess) return ens_fail(PFS_ERR_CUDA, cudaGetErrorString(e_)); \
+    } while (0)
+
+int build_tasks(Ensemble &E)
+{
+    std::vector<int> rowm, swm, rsm;
+    const int ow = 128 - 2 * E.halo;
+    for (int k = 0; k < E.n; ++k) {
+        Member &m = E.hmem[k];
+        m.row_task0 = (int)rowm.size();
+        m.nrow = (m.h + kRowsPerTask - 1) / kRowsPerTask;
+        for (int t = 0; t < m.nrow; ++t) rowm.push_back(k);
+        m.sw_task0 = (int)swm.size();
+        m.nsx = (m.w + ow - 1) / ow;
+        m.nsy = (m.h + E.chunk - 1) / E.chunk;
+        for (int t = 0; t < m.nsx * m.nsy; ++t) swm.push_back(k);
+        m.rs_task0 = (int)rsm.size();
+        m.rsx = (m.w + 127) / 128;
+        m.rsy = (m.h + 7) / 8;
+        for (int t = 0; t < m.rsx * m.rsy; ++t) rsm.push_back(k);
+    }
+    E.nrow = (int)rowm.size();
+    E.nsw = (int)swm.size();
+    E.nrs = (int)rsm.size();
+    if (E.dtasks) cudaFree(E.dtasks);
+    if (E.dparts) cudaFree(E.dparts);
+    E.dtasks = nullptr;
+    E.dparts = nullptr;
+    ECK(cudaMalloc(&E.dtasks, sizeof(int) * (E.nrow + E.nsw + E.nrs)));
+    ECK(cudaMemcpy(E.dtasks, rowm.data(), sizeof(int) * E.nrow, cudaMemcpyHostToDevice));
+    ECK(cudaMemcpy(E.dtasks + E.nrow, swm.data(), sizeof(int) * E.nsw, cudaMemcpyHostToDevice));
+    ECK(cudaMemcpy(E.dtasks + E.nrow + E.nsw, rsm.data(), sizeof(int) * E.nrs, cudaMemcpyHostToDevice));
+    ECK(cudaMalloc(&E.dparts, sizeof(double) * (E.nrow + E.nrs)));
+    ECK(cudaMemcpy(E.dmem, E.hmem.data(), sizeof(Member) * E.n, cudaMemcpyHostToDevice));
+    return PFS_OK;
+}
+
+template <int G, int L>
+cudaError_t launch_ens(const EnsArgs &a, int grid, cudaStream_t st)
+{
+    constexpr int smem = Ring<float, L>::bytes_per_block;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_ensemble_step<G, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr_coop;
+    attr_coop.id = cudaLaunchAttributeCooperative;
+    attr_coop.val.cooperative = 1;
+    cfg.attrs = &attr_coop;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_ensemble_step<G, L>, a);
+    if (e == cudaSuccess) launched();
+    return e;
+}
+
+int grid_for(Ensemble &E)
+{
+    int dev, sms, per = 0;
+    ECK(cudaGetDevice(&dev));
+    ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (E.levels == 8) {
+        cudaFuncSetAttribute(k_ensemble_step<8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Ring<float, 8>::bytes_per_block);
+        ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble_step<8, 8>, 128,
+                                                          Ring<float, 8>::bytes_per_block));
+    } else {
+        cudaFuncSetAttribute(k_ensemble_step<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             Ring<float, 4>::bytes_per_block);
+        ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble_step<4, 4>, 128,
+                                                          Ring<float, 4>::bytes_per_block));
+    }
+    if (per < 1) return ens_fail(PFS_ERR_UNSUPPORTED, "ensemble kernel does not fit on an SM");
+    E.grid = per * sms;
+    return PFS_OK;
+}
+
+EnsArgs make_args(Ensemble &E, int icur)
+{
+    EnsArgs a;
+    a.mem = E.dmem;
+    a.state = E.dstate;
+    a.nmem = E.n;
+    a.row_member = E.dtasks;
+    a.sw_member = E.dtasks + E.nrow;
+    a.rs_member = E.dtasks + E.nrow + E.nsw;
+    a.nrow_tasks = E.nrow;
+    a.nsw_tasks = E.nsw;
+    a.nrs_tasks = E.nrs;
+    a.row_part = E.dparts;
+    a.rs_part = E.dparts + E.nrow;
+    a.bar_count = E.dbar;
+    a.bar_gen = E.dbar + 1;
+    a.err = E.derr;
+    a.active = E.dactive;
+    a.dt = E.prm.dt;
+    a.gamma = (float)(-1.0 / (double)E.prm.dt);
+    a.tol = E.prm.tol > 0.0 ? E.prm.tol : -1.0;
+    a.cap = E.prm.max_iters;
+    a.check_every = E.prm.check_every > 0 ? E.prm.check_every : E.prm.max_iters;
+    a.chunk = E.chunk;
+    a.channels = E.c;
+    a.icur = icur;
+    return a;
+}
+
+int enqueue_step(Ensemble &E, int icur, cudaStream_t st)
+{
+    const int nchecks = E.prm.max_iters / E.levels + 2;
+    ECK(cudaMemsetAsync(E.dactive, 0, sizeof(int) * nchecks, st));
+    ECK(cudaMemsetAsync(E.dbar, 0, sizeof(unsigned) * 2, st));
+    const EnsArgs a = make_args(E, icur);
+    const cudaError_t e = E.levels == 8 ? launch_ens<8, 8>(a, E.grid, st) : launch_ens<4, 4>(a, E.grid, st);
+    ECK(e);
+    return PFS_OK;
+}
+
+void drop_graphs(Ensemble &E)
+{
+    for (auto &g : E.graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+// One CUDA graph per image parity: the step's two memsets and the kernel.
+int build_graphs(Ensemble &E)
+{
+    drop_graphs(E);
+    if (!E.graphs_ok) return PFS_OK;
+    cudaStream_t cs;
+    ECK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    for (int par = 0; par < 2; ++par) {
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        int rc = PFS_OK;
+        if (e == cudaSuccess) rc = enqueue_step(E, par, cs);
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        if (e == cudaSuccess && rc == PFS_OK && e2 == cudaSuccess) e = cudaGraphInstantiate(&E.graph[par], g, 0);
+        else e = cudaErrorStreamCaptureUnsupported;
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {  // no graph support for this launch: run it directly
+            cudaGetLastError();
+            E.graphs_ok = false;
+            drop_graphs(E);
+            break;
+        }
+    }
+    cudaStreamDestroy(cs);
+    return PFS_OK;
+}
+
+}  // namespace
+
+}  // namespace pfs
+
+using pfs::Ensemble;
+
+extern "C" {
+
+int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, int channels, const pfs_params *params,
+                        void *stream)
+{
+    if (!out || n <= 0 || !w || !h || !params || channels < 0)
+        return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad ensemble arguments");
+    *out = nullptr;
+    const pfs_params &p = *params;
+    if (!(p.dt > 0.0f) || p.viscosity != 0.0f || p.diffuse_iters < 2 || p.diffuse_iters % 2 ||
+        p.precision != PFS_PREC_F32)
+        return pfs::record_error(PFS_ERR_UNSUPPORTED,
+                                 "ensembles run float32 steps with viscosity 0 and an even diffusion count >= 2");
+    const int L = p.fuse_depth > 0 ? p.fuse_depth : 8;
+    if (L != 4 && L != 8) return pfs::record_error(PFS_ERR_UNSUPPORTED, "ensemble fuse_depth must be 4 or 8");
+    if (p.max_iters <= 0 || p.max_iters % L || (p.check_every > 0 && p.check_every % L))
+        return pfs::record_error(PFS_ERR_UNSUPPORTED, "ensemble sweep cap and check interval must be multiples of "
+                                                      "the fuse depth");
+    for (int k = 0; k < n; ++k)
+        if (w[k] <= 0 || h[k] <= 0 || w[k] % 4)
+            return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "member widths must be positive multiples of 4");
+    Ensemble *E = new (std::nothrow) Ensemble();
+    if (!E) return pfs::record_error(PFS_ERR_CUDA, "out of host memory");
+    E->n = n;
+    E->c = channels;
+    E->prm = p;
+    E->st = (cudaStream_t)stream;
+    E->levels = L;
+    E->halo = L == 8 ? 8 : 4;
+    E->chunk = p.chunk_rows > 0 ? p.chunk_rows : 32;
+    size_t tot = 0;
+    E->hmem.resize(n);
+    for (int k = 0; k < n; ++k) {
+        E->w.push_back(w[k]);
+        E->h.push_back(h[k]);
+        const int ld = (w[k] + 31) / 32 * 32;
+        E->ld.push_back(ld);
+        E->off.push_back(tot);
+        tot += (size_t)ld * h[k] * (7 + 2 * channels);
+    }
+    E->floats = tot;
+    int rc = PFS_OK;
+    auto bail = [&](int code) {
+        pfs_ensemble_destroy(reinterpret_cast<pfs_ensemble *>(E));
+        return code;
+    };
+    if (cudaMalloc(&E->mem, tot * sizeof(float)) != cudaSuccess || cudaMemset(E->mem, 0, tot * sizeof(float)))
+        return bail(pfs::record_error(PFS_ERR_CUDA, "ensemble allocation failed"));
+    for (int k = 0; k < n; ++k) {
+        pfs::Member &m = E->hmem[k];
+        m.w = w[k];
+        m.h = h[k];
+        m.ld = E->ld[k];
+        const size_t P = (size_t)m.ld * m.h;
+        float *q = E->mem + E->off[k];
+        m.u[0] = q;
+        m.u[1] = q + P;
+        m.v[0] = q + 2 * P;
+        m.v[1] = q + 3 * P;
+        m.p[0] = q + 4 * P;
+        m.p[1] = q + 5 * P;
+        m.b = q + 6 * P;
+        m.img[0] = q + 7 * P;
+        m.img[1] = q + (7 + channels) * P;
+    }
+    if (cudaMalloc(&E->dmem, sizeof(pfs::Member) * n) != cudaSuccess ||
+        cudaMalloc(&E->dstate, sizeof(pfs::MemberState) * n) != cudaSuccess ||
+        cudaMemset(E->dstate, 0, sizeof(pfs::MemberState) * n) != cudaSuccess ||
+        cudaMalloc(&E->dbar, 2 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&E->derr, sizeof(int)) != cudaSuccess || cudaMemset(E->derr, 0, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&E->dactive, sizeof(int) * (p.max_iters / 4 + 2)) != cudaSuccess)  // any fuse depth (>= 4)
+        return bail(pfs::record_error(PFS_ERR_CUDA, "ensemble allocation failed"));
+    if ((rc = pfs::build_tasks(*E)) != PFS_OK) return bail(rc);
+    if ((rc = pfs::grid_for(*E)) != PFS_OK) return bail(rc);
+    *out = reinterpret_cast<pfs_ensemble *>(E);
+    return PFS_OK;
+}
+
+int pfs_ensemble_destroy(pfs_ensemble *e)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E) return PFS_OK;
+    cudaStreamSynchronize(E->st);
+    pfs::drop_graphs(*E);
+    cudaFree(E->mem);
+    cudaFree(E->dmem);
+    cudaFree(E->dstate);
+    cudaFree(E->dtasks);
+    cudaFree(E->dparts);
+    cudaFree(E->dbar);
+    cudaFree(E->derr);
+    cudaFree(E->dactive);
+    cudaFree(E->stage);
+    cudaFree(E->snap);
+    cudaFree(E->snap_state);
+    delete E;
+    return PFS_OK;
+}
+
+int pfs_ensemble_snapshot(pfs_ensemble *e, int restore)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "null ensemble");
+    const size_t bytes = E->floats * sizeof(float), sbytes = sizeof(pfs::MemberState) * E->n;
+    cudaError_t r = cudaSuccess;
+    if (!restore) {
+        if (!E->snap) r = cudaMalloc(&E->snap, bytes);
+        if (r == cudaSuccess && !E->snap_state) r = cudaMalloc(&E->snap_state, sbytes);
+        if (r == cudaSuccess) r = cudaMemcpyAsync(E->snap, E->mem, bytes, cudaMemcpyDeviceToDevice, E->st);
+        if (r == cudaSuccess) r = cudaMemcpyAsync(E->snap_state, E->dstate, sbytes, cudaMemcpyDeviceToDevice, E->st);
+        E->snap_icur = E->icur;
+    } else {
+        if (!E->snap) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "no snapshot taken");
+        r = cudaMemcpyAsync(E->mem, E->snap, bytes, cudaMemcpyDeviceToDevice, E->st);
+        if (r == cudaSuccess) r = cudaMemcpyAsync(E->dstate, E->snap_state, sbytes, cudaMemcpyDeviceToDevice, E->st);
+        E->icur = E->snap_icur;
+    }
+    if (r == cudaSuccess) r = cudaStreamSynchronize(E->st);
+    return r == cudaSuccess ? PFS_OK : pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
+}
+
+static int ens_stage(Ensemble *E, size_t bytes)
+{
+    if (E->stage_bytes >= bytes) return PFS_OK;
+    cudaFree(E->stage);
+    E->stage = nullptr;
+    E->stage_bytes = 0;
+    if (cudaMalloc(&E->stage, bytes) != cudaSuccess) return pfs::record_error(PFS_ERR_CUDA, "staging allocation");
+    E->stage_bytes = bytes;
+    return PFS_OK;
+}
+
+int pfs_ensemble_upload(pfs_ensemble *e, int k, const float *vp, const float *tmp, const float *image, int where)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || k < 0 || k >= E->n || !vp || !tmp || (E->c > 0 && !image))
+        return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad ensemble upload arguments");
+    const pfs::Member &m = E->hmem[k];
+    const size_t nv = (size_t)m.w * m.h * 4, ni = (size_t)m.w * m.h * E->c;
+    const float *A = vp, *B = tmp, *I = image;
+    if (where == PFS_HOST) {
+        int rc = ens_stage(E, (2 * nv + ni) * sizeof(float));
+        if (rc != PFS_OK) return rc;
+        cudaMemcpyAsync(E->stage, vp, nv * 4, cudaMemcpyHostToDevice, E->st);
+        cudaMemcpyAsync(E->stage + nv, tmp, nv * 4, cudaMemcpyHostToDevice, E->st);
+        if (ni) cudaMemcpyAsync(E->stage + 2 * nv, image, ni * 4, cudaMemcpyHostToDevice, E->st);
+        A = E->stage;
+        B = E->stage + nv;
+        I = E->stage + 2 * nv;
+    }
+    cudaError_t r = pfs::launch_split_velocity(A, m.u[0], m.v[0], m.ld, m.w, m.h, E->st);
+    if (r == cudaSuccess) r = pfs::launch_split_channel(B, 2, 4, m.p[0], m.ld, m.w, m.h, E->st);
+    if (r == cudaSuccess && E->c > 0)
+        r = pfs::launch_split_image(I, m.img[E->icur], (size_t)m.ld * m.h, m.ld, m.w, m.h, E->c, E->st);
+    pfs::MemberState ms{};
+    if (r == cudaSuccess) r = cudaMemcpyAsync(E->dstate + k, &ms, sizeof ms, cudaMemcpyHostToDevice, E->st);
+    if (r == cudaSuccess && where == PFS_HOST) r = cudaStreamSynchronize(E->st);
+    if (r == cudaSuccess && where != PFS_HOST) r = cudaStreamSynchronize(E->st);  // ms lives on this stack frame
+    return r == cudaSuccess ? PFS_OK : pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
+}
+
+int pfs_ensemble_step(pfs_ensemble *e, int steps)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || steps < 0) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad ensemble step arguments");
+    if (E->graphs_ok && !E->graph[0]) {
+        int rc = pfs::build_graphs(*E);
+        if (rc != PFS_OK) return rc;
+    }
+    for (int s = 0; s < steps; ++s) {
+        cudaError_t r;
+        if (E->graphs_ok && E->graph[E->icur]) {
+            r = cudaGraphLaunch(E->graph[E->icur], E->st);
+            if (r == cudaSuccess) pfs::launched();
+        } else {
+            int rc = pfs::enqueue_step(*E, E->icur, E->st);
+            if (rc != PFS_OK) return rc;
+            r = cudaSuccess;
+        }
+        if (r != cudaSuccess) return pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
+        E->icur = 1 - E->icur;
+        E->steps += 1;
+    }
+    int err = 0;
+    cudaError_t r = cudaMemcpyAsync(&err, E->derr, sizeof(int), cudaMemcpyDeviceToHost, E->st);
+    if (r == cudaSuccess) r = cudaStreamSynchronize(E->st);
+    if (r != cudaSuccess) return pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
+    if (err) return pfs::record_error(PFS_ERR_DEVICE_TIMEOUT, "ensemble grid barrier timed out");
+    return PFS_OK;
+}
+
+int pfs_ensemble_member_stats(pfs_ensemble *e, int k, pfs_stats *out)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || k < 0 || k >= E->n || !out) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad arguments");
+    pfs::MemberState ms;
+    cudaError_t r = cudaMemcpyAsync(&ms, E->dstate + k, sizeof ms, cudaMemcpyDeviceToHost, E->st);
+    if (r == cudaSuccess) r = cudaStreamSynchronize(E->st);
+    if (r != cudaSuccess) return pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
+    std::memset(out, 0, sizeof *out);
+    out->sweeps = ms.sweeps;
+    out->checks = ms.checks;
+    out->rel_residual = ms.rel;
+    out->bnorm = std::sqrt(ms.bb);
+    out->capped = ms.capped;
+    out->steps = E->steps;
+    return PFS_OK;
+}
+
+int pfs_ensemble_download(pfs_ensemble *e, int k, float *vp, float *image, int where)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || k < 0 || k >= E->n) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad arguments");
+    const pfs::Member &m = E->hmem[k];
+    const size_t nv = (size_t)m.w * m.h * 4, ni = (size_t)m.w * m.h * E->c;
+    float *A = vp, *I = image;
+    if (where == PFS_HOST) {
+        int rc = ens_stage(E, (nv + ni) * sizeof(float));
+        if (rc != PFS_OK) return rc;
+        A = vp ? E->stage : nullptr;
+        I = image ? E->stage + nv : nullptr;
+    }
+    pfs::MemberState ms;
+    cudaError_t r = cudaMemcpyAsync(&ms, E->dstate + k, sizeof ms, cudaMemcpyDeviceToHost, E->st);
+    if (r == cudaSuccess) r = cudaStreamSynchronize(E->st);
+    if (r == cudaSuccess && A) r = pfs::launch_merge_velocity(A, m.u[0], m.v[0], m.p[ms.cur], m.b, m.ld, m.w, m.h, E->st);
+    if (r == cudaSuccess && I && E->c > 0)
+        r = pfs::launch_merge_image(I, m.img[E->icur], (size_t)m.ld * m.h, m.ld, m.w, m.h, E->c, E->st);
+    if (r == cudaSuccess && where == PFS_HOST) {
+        if (vp) r = cudaMemcpyAsync(vp, A, nv * 4, cudaMemcpyDeviceToHost, E->st);
+        if (r == cudaSuccess && image && ni) r = cudaMemcpyAsync(image, I, ni * 4, cudaMemcpyDeviceToHost, E->st);
+    }
+    if (r == cudaSuccess) r = cudaStreamSynchronize(E->st);
+    return r == cudaSuccess ? PFS_OK : pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
+}
+
+int pfs_ensemble_config(pfs_ensemble *e, int fuse_depth, int chunk_rows)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || (fuse_depth != 4 && fuse_depth != 8) || chunk_rows <= 0)
+        return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "fuse_depth 4 or 8, chunk_rows > 0");
+    if (E->prm.max_iters % fuse_depth || (E->prm.check_every > 0 && E->prm.check_every % fuse_depth))
+        return pfs::record_error(PFS_ERR_UNSUPPORTED, "cap / check interval not multiples of the fuse depth");
+    cudaStreamSynchronize(E->st);
+    E->levels = fuse_depth;
+    E->halo = fuse_depth == 8 ? 8 : 4;
+    E->chunk = chunk_rows;
+    E->prm.fuse_depth = fuse_depth;
+    E->prm.chunk_rows = chunk_rows;
+    pfs::drop_graphs(*E);
+    int rc = pfs::build_tasks(*E);
+    if (rc == PFS_OK) rc = pfs::grid_for(*E);
+    return rc;
+}
+
+int pfs_ensemble_info(pfs_ensemble *e, int *fuse_depth, int *chunk_rows, int *grid_blocks, int *graphs)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "null ensemble");
+    if (fuse_depth) *fuse_depth = E->levels;
+    if (chunk_rows) *chunk_rows = E->chunk;
+    if (grid_blocks) *grid_blocks = E->grid;
+    if (graphs) *graphs = E->graphs_ok && E->graph[0] ? 1 : 0;
+    return PFS_OK;
+}
+
+}  // extern "C"

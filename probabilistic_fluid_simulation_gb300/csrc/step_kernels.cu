@@ -7,6 +7,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
+#include "cells.cuh"
 
 namespace pfs {
 namespace {
@@ -15,44 +16,13 @@ constexpr int kBX = 32, kBY = 8;
 
 inline dim3 grid2d(int w, int h) { return dim3((w + kBX - 1) / kBX, (h + kBY - 1) / kBY); }
 
-__device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
-__device__ __forceinline__ int wp(int i, int n) { return i + 1 == n ? 0 : i + 1; }
-
-// Backtrace, wrap and corner cells of one sample (src/fluid.cpp:39-58 and
-// :97-114): x' = i - (k*u)/n wrapped to [0, n).
-struct Corners {
-    int i0, i1, j0, j1;
-    float sx, sy;
-};
-
-__device__ __forceinline__ Corners backtrace(int i, int j, float kx, float ky, float u, float v, float fw, float fh,
-                                            int w, int h)
-{
-    float xp = fsub((float)i, fdiv(fmul(kx, u), fw));
-    float yp = fsub((float)j, fdiv(fmul(ky, v), fh));
-    xp = wrap_coord(xp, fw);
-    yp = wrap_coord(yp, fh);
-    Corners c;
-    c.i0 = cell_of(xp, w);
-    c.j0 = cell_of(yp, h);
-    c.i1 = (c.i0 + 1) % w;
-    c.j1 = (c.j0 + 1) % h;
-    c.sx = fsub(xp, (float)c.i0);
-    c.sy = fsub(yp, (float)c.j0);
-    return c;
-}
-
 // src/fluid.cpp:24-70
 __global__ void k_advect(const float *__restrict__ u, const float *__restrict__ v, float *__restrict__ uo,
                          float *__restrict__ vo, int ld, int w, int h, float dt)
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    const size_t o = (size_t)j * ld + i;
-    const Corners c = backtrace(i, j, dt, dt, u[o], v[o], (float)w, (float)h, w, h);
-    const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
-    uo[o] = bilerp(c.sx, c.sy, u[r0 + c.i0], u[r0 + c.i1], u[r1 + c.i0], u[r1 + c.i1]);
-    vo[o] = bilerp(c.sx, c.sy, v[r0 + c.i0], v[r0 + c.i1], v[r1 + c.i0], v[r1 + c.i1]);
+    advect_cell(u, v, uo, vo, ld, w, h, dt, i, j);
 }
 
 // One diffusion sweep, src/fluid.cpp:151-186
@@ -75,40 +45,9 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ u,
 {
     FFAcc acc;
     for (int j = blockIdx.x; j < h; j += gridDim.x) {
-        const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
-        for (int i = threadIdx.x; i < w; i += blockDim.x) {
-            const float du = fsub(u[r + wp(i, w)], u[r + wm(i, w)]);
-            const float dv = fsub(v[rp + i], v[rm + i]);
-            const float bv = fmul(gamma, fadd(du, dv));
-            b[r + i] = bv;
-            acc_square(acc, bv);
-        }
+        for (int i = threadIdx.x; i < w; i += blockDim.x) acc_square(acc, divergence_cell(u, v, b, ld, w, h, gamma, i, j));
     }
     reduce_blocks(acc.value(), red, 1);
-}
-
-// Residual of the pressure system (src/fluid.cpp:239-257 solves 4p - sum nb = b),
-// r = b + pL + pR + pT + pB - 4p. The five additions are error-free (TwoSum),
-// so hi + lo carries r with a relative error near 2^-48 (the error terms are
-// summed in float). r^2 = hi^2 + (fma error of hi^2) + 2 hi lo is added to
-// the float-float accumulator.
-__device__ __forceinline__ void residual_sq(FFAcc &acc, float b, float l, float r, float t, float bo, float c)
-{
-    FF s = two_sum(b, l);
-    float e = s.lo;
-    s = two_sum(s.hi, r);
-    e = __fadd_rn(e, s.lo);
-    s = two_sum(s.hi, t);
-    e = __fadd_rn(e, s.lo);
-    s = two_sum(s.hi, bo);
-    e = __fadd_rn(e, s.lo);
-    s = two_sum(s.hi, __fmul_rn(-4.0f, c));  // -4p is exact
-    e = __fadd_rn(e, s.lo);
-    const FF q = two_sum(s.hi, e);
-    const float sq = __fmul_rn(q.hi, q.hi);
-    const float sq_err = __fmaf_rn(q.hi, q.hi, -sq);
-    const float cross = __fmul_rn(__fmul_rn(2.0f, q.hi), q.lo);
-    acc.add(sq, __fadd_rn(sq_err, cross));
 }
 
 __global__ void __launch_bounds__(256) k_residual(const float *__restrict__ p, const float *__restrict__ b, int ld,
@@ -161,38 +100,8 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *
     FFAcc acc[4], accb;  // one accumulator per lane column: four independent chains
     for (int wid = blockIdx.x * kResWarps + (threadIdx.x >> 5); wid < nwork; wid += gridDim.x * kResWarps) {
         const int sx = wid % nsx, sy = wid / nsx;
-        const int x = sx * 128 + 4 * lane;
-        const bool active = x < w;
-        const int xs = active ? x : w - 4;  // inactive lanes shadow a valid column, results discarded
-        const int last_lane = min(31, (w - sx * 128) / 4 - 1);
-        const int xl = (sx * 128 == 0) ? w - 1 : sx * 128 - 1;         // left outside neighbour
-        const int xr = (sx * 128 + 4 * (last_lane + 1)) % w;           // right outside neighbour
         const int y0 = sy * kResChunk, y1 = min(h, y0 + kResChunk);
-        const float *pc = p + xs;
-        float4 up = *reinterpret_cast<const float4 *>(pc + (size_t)wm(y0, h) * ld);
-        float4 cu = *reinterpret_cast<const float4 *>(pc + (size_t)y0 * ld);
-        for (int y = y0; y < y1; ++y) {
-            const float4 dn = *reinterpret_cast<const float4 *>(pc + (size_t)wp(y, h) * ld);
-            const float4 bb = *reinterpret_cast<const float4 *>(b + (size_t)y * ld + xs);
-            float lft = __shfl_up_sync(0xffffffffu, cu.w, 1);
-            float rgt = __shfl_down_sync(0xffffffffu, cu.x, 1);
-            if (lane == 0) lft = p[(size_t)y * ld + xl];
-            if (lane == last_lane) rgt = p[(size_t)y * ld + xr];
-            if (active) {
-                residual_sq(acc[0], bb.x, lft, cu.y, up.x, dn.x, cu.x);
-                residual_sq(acc[1], bb.y, cu.x, cu.z, up.y, dn.y, cu.y);
-                residual_sq(acc[2], bb.z, cu.y, cu.w, up.z, dn.z, cu.z);
-                residual_sq(acc[3], bb.w, cu.z, rgt, up.w, dn.w, cu.w);
-                if (with_b) {
-                    acc_square(accb, bb.x);
-                    acc_square(accb, bb.y);
-                    acc_square(accb, bb.z);
-                    acc_square(accb, bb.w);
-                }
-            }
-            up = cu;
-            cu = dn;
-        }
+        residual_strip_task(p, b, ld, w, h, sx, y0, y1, lane, acc, with_b ? &accb : nullptr);
     }
     reduce_blocks((acc[0].value() + acc[1].value()) + (acc[2].value() + acc[3].value()), red, 0, state, sweeps_here,
                   tol);
@@ -200,18 +109,6 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *
         __syncthreads();
         reduce_blocks(accb.value(), red, 1);
     }
-}
-
-// Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2.
-__device__ __forceinline__ void project_cell(const float *__restrict__ u, const float *__restrict__ v,
-                                             const float *__restrict__ p, int ld, int w, int h, float dt, int i,
-                                             int j, float &uo, float &vo)
-{
-    const size_t r = (size_t)j * ld;
-    const float gx = fmul(fmul(fsub(p[r + wp(i, w)], p[r + wm(i, w)]), dt), 0.5f);
-    const float gy = fmul(fmul(fsub(p[(size_t)wp(j, h) * ld + i], p[(size_t)wm(j, h) * ld + i]), dt), 0.5f);
-    uo = fsub(u[r + i], gx);
-    vo = fsub(v[r + i], gy);
 }
 
 __global__ void k_project(const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ p,
@@ -236,18 +133,7 @@ __global__ void k_project_advect_image(const float *__restrict__ u, const float 
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    float un, vn;
-    project_cell(u, v, p, ld, w, h, dt, i, j, un, vn);
-    const size_t o = (size_t)j * ld + i;
-    uo[o] = un;
-    vo[o] = vn;
-    // dt / viw with viw = 1.0f is dt exactly
-    const Corners k = backtrace(i, j, dt, dt, un, vn, (float)w, (float)h, w, h);
-    const size_t r0 = (size_t)k.j0 * ld, r1 = (size_t)k.j1 * ld;
-    for (int ch = 0; ch < c; ++ch) {
-        const float *s = img + ch * plane;
-        imgo[ch * plane + o] = bilerp(k.sx, k.sy, s[r0 + k.i0], s[r0 + k.i1], s[r1 + k.i0], s[r1 + k.i1]);
-    }
+    project_image_cell(u, v, p, uo, vo, ld, w, h, dt, img, imgo, plane, c, i, j);
 }
 
 // Image advection, src/fluid.cpp:72-127, planar image and velocity.

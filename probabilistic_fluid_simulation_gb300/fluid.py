@@ -91,6 +91,17 @@ SIGNATURES = [
     ("pfs_session_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("pfs_session_sync", C.c_int, [C.c_void_p]),
     ("pfs_session_destroy", C.c_int, [C.c_void_p]),
+    ("pfs_ensemble_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
+                                      C.POINTER(Params), C.c_void_p]),
+    ("pfs_ensemble_upload", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    ("pfs_ensemble_step", C.c_int, [C.c_void_p, C.c_int]),
+    ("pfs_ensemble_download", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    ("pfs_ensemble_member_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Stats)]),
+    ("pfs_ensemble_config", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("pfs_ensemble_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]),
+    ("pfs_ensemble_snapshot", C.c_int, [C.c_void_p, C.c_int]),
+    ("pfs_ensemble_destroy", C.c_int, [C.c_void_p]),
     ("pfs_pressure_sweeps", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                       C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("pfs_residual_norms", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
@@ -266,6 +277,73 @@ class Session:
     def close(self):
         if self._h:
             lib().pfs_session_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Ensemble:
+    """Many independent simulations in one persistent kernel per timestep
+    (pfs_ensemble_* in include/pfs.h). sizes: list of (w, h)."""
+
+    def __init__(self, sizes, channels: int, params: Optional[Params] = None, stream: int = 0, **kw):
+        self._h = C.c_void_p()
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        self.channels = channels
+        self.params = params if params is not None else default_params(**kw)
+        n = len(self.sizes)
+        ws = (C.c_int * n)(*[w for w, _ in self.sizes])
+        hs = (C.c_int * n)(*[h for _, h in self.sizes])
+        _check(lib().pfs_ensemble_create(C.byref(self._h), n, ws, hs, channels, C.byref(self.params),
+                                         C.c_void_p(stream or None)))
+
+    def upload(self, k: int, vp, tmp, image=None):
+        where = PFS_HOST if isinstance(vp, np.ndarray) else PFS_DEVICE
+        _check(lib().pfs_ensemble_upload(self._h, k, C.c_void_p(_ptr(vp)), C.c_void_p(_ptr(tmp)),
+                                         C.c_void_p(_ptr(image) if image is not None else None), where))
+
+    def step(self, n: int = 1):
+        _check(lib().pfs_ensemble_step(self._h, int(n)))
+
+    def download(self, k: int, vp=None, image=None):
+        ref = vp if vp is not None else image
+        where = PFS_HOST if isinstance(ref, np.ndarray) else PFS_DEVICE
+        _check(lib().pfs_ensemble_download(self._h, k, C.c_void_p(_ptr(vp) if vp is not None else None),
+                                           C.c_void_p(_ptr(image) if image is not None else None), where))
+        return vp, image
+
+    def stats(self, k: int) -> dict:
+        s = Stats()
+        _check(lib().pfs_ensemble_member_stats(self._h, k, C.byref(s)))
+        return s.as_dict()
+
+    def config(self, fuse_depth: int, chunk_rows: int):
+        _check(lib().pfs_ensemble_config(self._h, int(fuse_depth), int(chunk_rows)))
+
+    def snapshot(self):
+        _check(lib().pfs_ensemble_snapshot(self._h, 0))
+
+    def restore(self):
+        _check(lib().pfs_ensemble_snapshot(self._h, 1))
+
+    def info(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        _check(lib().pfs_ensemble_info(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("fuse_depth", "chunk_rows", "grid_blocks", "graphs"), [x.value for x in v]))
+
+    def close(self):
+        if self._h:
+            lib().pfs_ensemble_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

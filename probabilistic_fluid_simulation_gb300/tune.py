@@ -57,6 +57,36 @@ def best_config(size: int, height: int = 0, levels=LEVELS, chunks=CHUNKS, reps: 
     return best
 
 
+ENSEMBLE_CANDIDATES = ((8, 16), (8, 24), (8, 32), (8, 48), (4, 16), (4, 32), (4, 64))
+
+
+def tune_ensemble(ens, steps: int = 1, candidates=ENSEMBLE_CANDIDATES):
+    """Pick the ensemble's (fuse depth, chunk rows) by timing `steps` steps
+    per candidate, each from the ensemble's current state (snapshot taken
+    first, restored before every trial and at the end); leaves the fastest
+    configured. Returns (best, timings), timings = [(fuse, chunk, ms/step)]."""
+    import torch
+    p = ens.params
+    timings = []
+    ens.snapshot()
+    for fuse, chunk in candidates:
+        if p.max_iters % fuse or (p.check_every > 0 and p.check_every % fuse):
+            continue
+        ens.config(fuse, chunk)
+        ens.restore()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ens.step(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        timings.append((fuse, chunk, e0.elapsed_time(e1) / steps))
+    best = min(timings, key=lambda t: t[2])
+    ens.config(best[0], best[1])
+    ens.restore()
+    return best, timings
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, default=2048)

@@ -1,0 +1,99 @@
+"""Batched form: members of an ensemble (one persistent cooperative kernel per
+timestep for all of them) against plain sessions with the same parameters,
+bit for bit."""
+import numpy as np
+import pytest
+
+from probabilistic_fluid_simulation_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(64, 64), (128, 64), (64, 256), (256, 128), (96, 40), (128, 128), (192, 96), (64, 128), (256, 256),
+         (32, 48), (8, 8), (520, 64)]
+
+
+def member_state(w, h, k):
+    base = S.draw_vortices(256, 256, seed=99)
+    vort = [S.Vortex(v.cx * w / 256, v.cy * h / 256, v.radius * (w * h) ** 0.5 / 256, v.circulation)
+            for v in S.perturb_vortices(base, seed=99, member=k)]
+    vp = S.velocity_from_vortices(w, h, vort)
+    tmp = np.zeros_like(vp)
+    img = S.blob_image(w, h, 3, seed=k)
+    return vp, tmp, img
+
+
+def session_run(pfs_lib, vp, tmp, img, steps, **kw):
+    h, w, _ = vp.shape
+    with pfs_lib.Session(w, h, image_shape=img.shape, **kw) as s:
+        s.upload(vp, tmp, img)
+        stats = []
+        for _ in range(steps):
+            s.step(1)
+            stats.append(s.stats())
+        a, b, c = np.empty_like(vp), np.empty_like(vp), np.empty_like(img)
+        s.download(a, b, c)
+    return a, b, c, stats
+
+
+@pytest.mark.parametrize("fuse,chunk,tol,every,cap", [(8, 32, 0.0, 0, 96), (8, 24, 1e-3, 32, 2400),
+                                                      (4, 16, 1e-3, 48, 2400)])
+def test_ensemble_members_equal_sessions(cuda_device, pfs_lib, fuse, chunk, tol, every, cap):
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=cap, tol=tol, check_every=every, fuse_depth=fuse, chunk_rows=chunk)
+    states = [member_state(w, h, k) for k, (w, h) in enumerate(SIZES)]
+    steps = 3
+    with pfs_lib.Ensemble(SIZES, 3, **kw) as ens:
+        for k, (vp, tmp, img) in enumerate(states):
+            ens.upload(k, vp, tmp, img)
+        per_step = []
+        for _ in range(steps):
+            ens.step(1)
+            per_step.append([ens.stats(k) for k in range(len(SIZES))])
+        info = ens.info()
+        outs = []
+        for k, (vp, tmp, img) in enumerate(states):
+            a, c = np.empty_like(vp), np.empty_like(img)
+            ens.download(k, a, c)
+            outs.append((a, c))
+    print("ensemble info", info)
+    assert info["fuse_depth"] == fuse and info["chunk_rows"] == chunk
+    sweeps_seen = set()
+    for k, (vp, tmp, img) in enumerate(states):
+        sa, sb, sc, sst = session_run(pfs_lib, vp, tmp, img, steps, **kw)
+        a, c = outs[k]
+        assert np.array_equal(a[..., 0:2], sa[..., 0:2]), (k, SIZES[k])
+        assert np.array_equal(a[..., 2], sb[..., 2]), (k, SIZES[k])  # final pressure
+        assert np.array_equal(a[..., 3], sa[..., 3]), (k, SIZES[k])
+        assert np.array_equal(c, sc), (k, SIZES[k])
+        for step in range(steps):
+            e, s = per_step[step][k], sst[step]
+            assert e["sweeps"] == s["sweeps"], (k, step, e, s)
+            assert e["capped"] == s["capped"]
+            if tol > 0:
+                assert e["rel_residual"] == pytest.approx(s["rel_residual"], rel=1e-9)
+            sweeps_seen.add(e["sweeps"])
+    if tol > 0:
+        assert len(sweeps_seen) > 2  # members converge at different sweep counts
+
+
+def test_ensemble_autotuner_keeps_results(cuda_device, pfs_lib):
+    from probabilistic_fluid_simulation_gb300 import tune
+    sizes = SIZES[:6]
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=96, tol=0.0, check_every=0)
+    states = [member_state(w, h, k) for k, (w, h) in enumerate(sizes)]
+    with pfs_lib.Ensemble(sizes, 3, **kw) as ens:
+        for k, st in enumerate(states):
+            ens.upload(k, *st)
+        best, timings = tune.tune_ensemble(ens, steps=1)
+        assert len(timings) >= 4 and best in timings
+        ens.step(2)
+        a, c = np.empty_like(states[3][0]), np.empty_like(states[3][2])
+        ens.download(3, a, c)
+    sa, sb, sc, _ = session_run(pfs_lib, *states[3], 2, **kw)
+    assert np.array_equal(a[..., 0:2], sa[..., 0:2]) and np.array_equal(c, sc)
+
+
+def test_ensemble_rejects_unsupported(cuda_device, pfs_lib):
+    with pytest.raises(pfs_lib.PFSError):
+        pfs_lib.Ensemble([(64, 64)], 3, dt=0.1, diffuse_iters=2, max_iters=100)  # cap not a multiple of 8
+    with pytest.raises(pfs_lib.PFSError):
+        pfs_lib.Ensemble([(66, 64)], 3, dt=0.1, diffuse_iters=2, max_iters=96)  # width not a multiple of 4
