@@ -169,6 +169,8 @@ typedef struct {
     long long steps;     /* steps run by this session                       */
     long long total_sweeps;
     long long cap_hits;
+    int start_kind;      /* initial pressure of the last step: PFS_START_* */
+    double rel_start;    /* relative residual of that initial pressure (-1 if not evaluated) */
 } pfs_stats;
 
 typedef struct pfs_session pfs_session;
@@ -193,6 +195,45 @@ int pfs_session_download_f64(pfs_session *s, double *vp, double *image, int wher
 int pfs_session_stats(pfs_session *s, pfs_stats *out);
 int pfs_session_sync(pfs_session *s);
 int pfs_session_destroy(pfs_session *s);
+
+/* ---- learned warm start -------------------------------------------------------------- */
+/*
+ * A 4-level U-Net (3x3 circular convolutions, 16/32/64/64 channels, bf16
+ * weights and activations, fp32 accumulation) mapping the divergence of a
+ * step, normalised by its rms, to the pressure, normalised the same way. Its
+ * forward and backward kernels are the library's own (tensor-core implicit
+ * GEMM convolutions); training is forward_backward + adam_step on batches of
+ * (b, p) pairs. Grids must have height and width multiples of 128. No
+ * counterpart in the reference (whose pressure iteration always starts from
+ * the previous pressure).
+ */
+typedef struct pfs_unet pfs_unet;
+/* buffers for up to max_pixels pixels per batch (images x height x width) */
+int pfs_unet_create(pfs_unet **out, long long max_pixels);
+int pfs_unet_destroy(pfs_unet *u);
+long long pfs_unet_num_params(pfs_unet *u);
+int pfs_unet_set_params(pfs_unet *u, const float *host_params);
+int pfs_unet_get_params(pfs_unet *u, float *host_params);
+int pfs_unet_get_grads(pfs_unet *u, float *host_grads);
+/* mean squared error of the prediction for n (b, p) pairs (dense float32
+ * device arrays, n x h x w, already normalised) and the gradients of all
+ * parameters; *loss receives the loss (blocking) if non-NULL */
+int pfs_unet_forward_backward(pfs_unet *u, const float *b, const float *p, int n, int h, int w, float *loss,
+                              void *stream);
+int pfs_unet_adam_step(pfs_unet *u, float lr, void *stream);
+/* p = rms(b) * net(b / rms(b)) for one plane (row pitches ldb, ldp floats) */
+int pfs_unet_predict(pfs_unet *u, const float *b, int ldb, float *p, int ldp, int h, int w, void *stream);
+
+/* Initial pressure of each step's iteration in a float32 session:
+ *   PFS_START_PREVIOUS  the previous step's pressure (the reference, default)
+ *   PFS_START_ZERO      zero
+ *   PFS_START_NETWORK   the network's prediction; if its residual is not
+ *                       below the previous pressure's, or the residual stops
+ *                       falling between checks, the iteration continues from
+ *                       the previous pressure (stats.start_kind then reads
+ *                       PFS_START_FALLBACK). The session keeps a pointer to u. */
+enum { PFS_START_PREVIOUS = 0, PFS_START_ZERO = 1, PFS_START_NETWORK = 2, PFS_START_FALLBACK = 3 };
+int pfs_session_set_start(pfs_session *s, int mode, pfs_unet *u);
 
 /* ---- ensembles: many independent simulations in one persistent kernel ------------ */
 /*

@@ -24,6 +24,7 @@
 #include "kernels.h"
 #include "pfs.h"
 #include "precision.h"
+#include "unet.h"
 
 using pfs::Reduce;
 
@@ -90,6 +91,7 @@ struct Field {
     double *hres = nullptr;  // pinned, [2]
     pfs::SolveState *dstate = nullptr;  // device
     pfs::SolveState *hstate = nullptr;  // pinned host copy
+    float *pback = nullptr;             // plain start kept aside while a predicted start is tried
     Reduce red{};
 
     int alloc(int w_, int h_)
@@ -133,6 +135,8 @@ struct Field {
         if (hres) cudaFreeHost(hres);
         if (dstate) cudaFree(dstate);
         if (hstate) cudaFreeHost(hstate);
+        if (pback) cudaFree(pback);
+        pback = nullptr;
         mem = nullptr;
         rmem = nullptr;
         hres = nullptr;
@@ -156,12 +160,16 @@ struct StepCfg {
     int check_every = 0;
     bool want_res = false;
     Tuning tun;
+    int start_mode = PFS_START_PREVIOUS;
+    pfs::unet::Net *net = nullptr;
 };
 
 struct StepOut {
     int sweeps = 0, checks = 0;
     double rel = -1.0, bnorm = -1.0;
     bool capped = false;
+    int start_kind = PFS_START_PREVIOUS;
+    double rel_start = -1.0;
 };
 
 bool fused_ok(const Field &f) { return f.w % 4 == 0; }
@@ -209,6 +217,9 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     int nmarks = 0, batch = 1, in_batch = 0;
     int S = 0;
     bool finished = false;
+    // predicted start: watch every check; if the residual does not fall, restart from the plain start
+    const bool watch = resid && o.start_kind == PFS_START_NETWORK;
+    double last_rel = o.rel_start;
     while (S < c.S && !finished) {
         int stop = c.S;
         if (resid && c.check_every > 0) stop = std::min(c.S, (S / c.check_every + 1) * c.check_every);
@@ -234,10 +245,17 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
         if (!resid) break;
         CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, st));
         marks[nmarks++] = {S, cur, prev};
-        if (++in_batch == batch || S == c.S || nmarks == 64) {
+        if (++in_batch == batch || S == c.S || nmarks == 64 || watch) {
             CK(cudaMemcpyAsync(f.hstate, f.dstate, sizeof(pfs::SolveState), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             if (f.hstate->done || S == c.S) finished = true;
+            if (watch && !finished && o.start_kind == PFS_START_NETWORK) {
+                if (!(f.hstate->rel < last_rel)) {  // the residual failed to fall: the plain start takes over
+                    CK(cudaMemcpyAsync(f.p[cur], f.pback, f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
+                    o.start_kind = PFS_START_FALLBACK;
+                }
+                last_rel = f.hstate->rel;
+            }
             if (nmarks == 64 && !finished) {  // keep the latest mark only
                 marks[0] = marks[63];
                 nmarks = 1;
@@ -309,6 +327,27 @@ int velocity_phase(Field &f, int vp, int tmp, const StepCfg &c, StepOut &o, cuda
     // computePressure(vp, tmp): src/fluid.cpp:303
     const float gamma = (float)(-1.0 / (double)c.dt);
     CK(pfs::launch_divergence(f.u[X], f.v[X], f.b, f.ld, f.w, f.h, gamma, f.red, st));
+    o.start_kind = c.start_mode;
+    if (c.start_mode == PFS_START_ZERO) {
+        CK(cudaMemsetAsync(f.p[f.pidx[X]], 0, f.plane * sizeof(float), st));
+    } else if (c.start_mode == PFS_START_NETWORK) {
+        if (!f.pback) CK(cudaMalloc(&f.pback, f.plane * sizeof(float)));
+        float *px = f.p[f.pidx[X]];
+        CK(cudaMemcpyAsync(f.pback, px, f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        CKS(pfs::unet::predict(c.net, f.b, f.ld, px, f.ld, f.h, f.w, st));
+        double rr, bb;
+        CKS(residual_host(f, px, st, rr, bb));
+        const double rel_net = relative(rr, bb);
+        CKS(residual_host(f, f.pback, st, rr, bb));
+        const double rel_plain = relative(rr, bb);
+        if (rel_net < rel_plain) {
+            o.rel_start = rel_net;
+        } else {  // the prediction is no better than the previous pressure: keep the plain start
+            CK(cudaMemcpyAsync(px, f.pback, f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            o.start_kind = PFS_START_FALLBACK;
+            o.rel_start = rel_plain;
+        }
+    }
     int cur = f.pidx[X], prev = f.pidx[Y];
     CKS(pressure_solve(f, X, Y, c, o, st, cur, prev));
     const int S = o.sweeps;
@@ -421,6 +460,8 @@ struct pfs_session {
     pfs_params prm{};
     pfs_stats stats{};
     pfs::LpState *lp = nullptr;  // precision forms other than F32
+    int start_mode = PFS_START_PREVIOUS;
+    pfs::unet::Net *net = nullptr;
     ~pfs_session()
     {
         if (img_mem) cudaFree(img_mem);
@@ -629,6 +670,8 @@ static StepCfg session_cfg(const pfs_session *s)
     if (s->prm.fuse_depth > 0) c.tun.levels = s->prm.fuse_depth;
     c.tun.halo = c.tun.levels <= 4 ? 4 : 8;
     if (s->prm.chunk_rows > 0) c.tun.chunk = s->prm.chunk_rows;
+    c.start_mode = s->start_mode;
+    c.net = s->net;
     return c;
 }
 
@@ -811,7 +854,25 @@ int pfs_session_step(pfs_session *s, int n)
         s->stats.steps += 1;
         s->stats.total_sweeps += o.sweeps;
         s->stats.cap_hits += o.capped ? 1 : 0;
+        s->stats.start_kind = o.start_kind;
+        s->stats.rel_start = o.rel_start;
     }
+    return PFS_OK;
+}
+
+int pfs_session_set_start(pfs_session *s, int mode, pfs_unet *u)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    if (mode < PFS_START_PREVIOUS || mode > PFS_START_NETWORK)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "start mode must be PFS_START_PREVIOUS, _ZERO or _NETWORK");
+    if (s->lp) return fail(PFS_ERR_UNSUPPORTED, "start modes apply to float32 sessions");
+    if (mode == PFS_START_NETWORK) {
+        if (!u) return fail(PFS_ERR_INVALID_ARGUMENT, "network start needs a network");
+        if (s->f.w % 128 || s->f.h % 128)
+            return fail(PFS_ERR_UNSUPPORTED, "network start needs grid sides that are multiples of 128");
+    }
+    s->start_mode = mode;
+    s->net = mode == PFS_START_NETWORK ? reinterpret_cast<pfs::unet::Net *>(u) : nullptr;
     return PFS_OK;
 }
 

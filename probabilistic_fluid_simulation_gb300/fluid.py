@@ -32,6 +32,7 @@ LIB_PATH = os.path.join(_PKG, "libpfs_gb300.so")
 PFS_HOST, PFS_DEVICE = 0, 1
 PREC_F32, PREC_BF16, PREC_F16, PREC_F64 = 0, 1, 2, 3
 PRECISIONS = {"f32": PREC_F32, "bf16": PREC_BF16, "f16": PREC_F16, "f64": PREC_F64}
+START_PREVIOUS, START_ZERO, START_NETWORK, START_FALLBACK = 0, 1, 2, 3
 
 
 class PFSError(RuntimeError):
@@ -55,7 +56,7 @@ class Stats(C.Structure):
     """pfs_stats (include/pfs.h)."""
     _fields_ = [("sweeps", C.c_int), ("checks", C.c_int), ("rel_residual", C.c_double), ("bnorm", C.c_double),
                 ("capped", C.c_int), ("steps", C.c_longlong), ("total_sweeps", C.c_longlong),
-                ("cap_hits", C.c_longlong)]
+                ("cap_hits", C.c_longlong), ("start_kind", C.c_int), ("rel_start", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -91,6 +92,18 @@ SIGNATURES = [
     ("pfs_session_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("pfs_session_sync", C.c_int, [C.c_void_p]),
     ("pfs_session_destroy", C.c_int, [C.c_void_p]),
+    ("pfs_unet_create", C.c_int, [C.POINTER(C.c_void_p), C.c_longlong]),
+    ("pfs_unet_destroy", C.c_int, [C.c_void_p]),
+    ("pfs_unet_num_params", C.c_longlong, [C.c_void_p]),
+    ("pfs_unet_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pfs_unet_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pfs_unet_get_grads", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pfs_unet_forward_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                            C.POINTER(C.c_float), C.c_void_p]),
+    ("pfs_unet_adam_step", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
+    ("pfs_unet_predict", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                   C.c_void_p]),
+    ("pfs_session_set_start", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("pfs_ensemble_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
                                       C.POINTER(Params), C.c_void_p]),
     ("pfs_ensemble_upload", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
@@ -271,6 +284,11 @@ class Session:
         _check(lib().pfs_session_stats(self._h, C.byref(s)))
         return s.as_dict()
 
+    def set_start(self, mode: int, net: "UNet" = None):
+        """Initial pressure of each step: START_PREVIOUS (reference), START_ZERO, START_NETWORK."""
+        self._net = net  # keep the network alive while the session uses it
+        _check(lib().pfs_session_set_start(self._h, int(mode), net._h if net is not None else None))
+
     def sync(self):
         _check(lib().pfs_session_sync(self._h))
 
@@ -290,6 +308,59 @@ class Session:
 
     def __exit__(self, *a):
         self.close()
+
+
+class UNet:
+    """The warm-start network (pfs_unet_* in include/pfs.h)."""
+
+    def __init__(self, max_pixels: int):
+        self._h = C.c_void_p()
+        _check(lib().pfs_unet_create(C.byref(self._h), int(max_pixels)))
+        self.n_params = lib().pfs_unet_num_params(self._h)
+
+    def set_params(self, params: np.ndarray):
+        params = np.ascontiguousarray(params, np.float32)
+        assert params.size == self.n_params
+        _check(lib().pfs_unet_set_params(self._h, C.c_void_p(params.ctypes.data)))
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        _check(lib().pfs_unet_get_params(self._h, C.c_void_p(out.ctypes.data)))
+        return out
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        _check(lib().pfs_unet_get_grads(self._h, C.c_void_p(out.ctypes.data)))
+        return out
+
+    def forward_backward(self, b, p, stream: int = 0) -> float:
+        """b, p: (n, h, w) float32 CUDA tensors (normalised pairs)."""
+        n, h, w = b.shape
+        loss = C.c_float()
+        _check(lib().pfs_unet_forward_backward(self._h, C.c_void_p(_ptr(b)), C.c_void_p(_ptr(p)), n, h, w,
+                                               C.byref(loss), C.c_void_p(stream or None)))
+        return loss.value
+
+    def adam_step(self, lr: float, stream: int = 0):
+        _check(lib().pfs_unet_adam_step(self._h, float(lr), C.c_void_p(stream or None)))
+
+    def predict(self, b, out, stream: int = 0):
+        """b, out: (h, w) float32 CUDA tensors: out = rms(b) * net(b / rms(b))."""
+        h, w = b.shape
+        _check(lib().pfs_unet_predict(self._h, C.c_void_p(_ptr(b)), w, C.c_void_p(_ptr(out)), w, h, w,
+                                      C.c_void_p(stream or None)))
+        return out
+
+    def close(self):
+        if self._h:
+            lib().pfs_unet_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Ensemble:
