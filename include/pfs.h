@@ -139,13 +139,21 @@ enum { PFS_HOST = 0, PFS_DEVICE = 1 };
  *   PFS_PREC_F16   the same with fp16 storage (the right-hand side of each
  *                  correction solve is scaled by 1/max|r| into fp16 range);
  *   PFS_PREC_F64   every field and operation in FP64: the FP64 run of the
- *                  same method, the yardstick for the others' error.
+ *                  same method, the yardstick for the others' error;
+ *   PFS_PREC_F32R  velocity, image and the pressure correction stored
+ *                  float32, the correction sweeps in FP32 (the fused sweep
+ *                  kernel of the F32 form), pressure and residual in FP64 by
+ *                  the same refinement as BF16 / F16. Unlike F32, whose float
+ *                  pressure cannot represent a solution below a relative
+ *                  residual of about 4.5 * 2^-25 * rms(p) / rms(b) (about
+ *                  1e-5 on a 256x256 vortex grid, more on larger ones), it
+ *                  reaches any tolerance the FP64 residual resolves.
  * The non-F32 forms run with viscosity 0 and an even diffusion count (the
  * reference's buffer roles then reduce to: pressure iteration from the
  * previous final pressure, projection with the final pressure); other
  * settings return PFS_ERR_UNSUPPORTED. check_every sets the sweeps between
- * refinements of the 16-bit forms (0 means 32). */
-enum { PFS_PREC_F32 = 0, PFS_PREC_BF16 = 1, PFS_PREC_F16 = 2, PFS_PREC_F64 = 3 };
+ * refinements of the refined forms (0 means 32). */
+enum { PFS_PREC_F32 = 0, PFS_PREC_BF16 = 1, PFS_PREC_F16 = 2, PFS_PREC_F64 = 3, PFS_PREC_F32R = 4 };
 
 typedef struct {
     float dt;
@@ -171,6 +179,7 @@ typedef struct {
     long long cap_hits;
     int start_kind;      /* initial pressure of the last step: PFS_START_* */
     double rel_start;    /* relative residual of that initial pressure (-1 if not evaluated) */
+    int start_passes;    /* damped passes applied to a predicted start in the last step    */
 } pfs_stats;
 
 typedef struct pfs_session pfs_session;
@@ -223,17 +232,43 @@ int pfs_unet_forward_backward(pfs_unet *u, const float *b, const float *p, int n
 int pfs_unet_adam_step(pfs_unet *u, float lr, void *stream);
 /* p = rms(b) * net(b / rms(b)) for one plane (row pitches ldb, ldp floats) */
 int pfs_unet_predict(pfs_unet *u, const float *b, int ldb, float *p, int ldp, int h, int w, void *stream);
+/* the same with the network run on the grid coarsened `coarsen` times: b
+ * averaged over coarsen x coarsen blocks, the prediction interpolated back
+ * (periodic bilinear, fine cell i at coarse coordinate (i + 1/2)/coarsen - 1/2)
+ * and scaled by coarsen^2 (the 5-point operator in cell units scales with the
+ * cell size squared). Lets a network trained at side N serve grids of side
+ * coarsen * N, whose features are coarsen times larger in cells. */
+int pfs_unet_predict_coarse(pfs_unet *u, const float *b, int ldb, float *p, int ldp, int h, int w, int coarsen,
+                            void *stream);
 
-/* Initial pressure of each step's iteration in a float32 session:
+/* Initial pressure of each step's iteration:
  *   PFS_START_PREVIOUS  the previous step's pressure (the reference, default)
  *   PFS_START_ZERO      zero
- *   PFS_START_NETWORK   the network's prediction; if its residual is not
- *                       below the previous pressure's, or the residual stops
- *                       falling between checks, the iteration continues from
- *                       the previous pressure (stats.start_kind then reads
- *                       PFS_START_FALLBACK). The session keeps a pointer to u. */
+ *   PFS_START_NETWORK   the network's prediction followed by
+ *                       PFS_START_DAMP_PASSES damped Jacobi passes
+ *                       p += (b - A p) / 8 (the undamped iteration cannot
+ *                       reduce the checkerboard component of an error, which
+ *                       a predicted start carries). If the residual of that
+ *                       start is not finite or above PFS_START_SLACK times the
+ *                       previous pressure's (a broken prediction), or the
+ *                       residual stops falling between checks, the iteration
+ *                       continues from the previous pressure (stats.start_kind
+ *                       then reads PFS_START_FALLBACK). The slack is there
+ *                       because the residual at the start overweights fine-scale
+ *                       error, which the sweeps remove within tens of sweeps;
+ *                       the sweeps needed are set by the smooth error. The
+ *                       session keeps a pointer to u. Not available in the F64
+ *                       form (the network reads float32 divergence). */
 enum { PFS_START_PREVIOUS = 0, PFS_START_ZERO = 1, PFS_START_NETWORK = 2, PFS_START_FALLBACK = 3 };
+enum { PFS_START_DAMP_PASSES = 8, PFS_START_SLACK = 4 };
 int pfs_session_set_start(pfs_session *s, int mode, pfs_unet *u);
+/* PFS_START_NETWORK with the network run on the grid coarsened `coarsen`
+ * times (pfs_unet_predict_coarse; 1 = the session's grid) and applied
+ * `passes` times (1..8): pass 1 predicts the pressure from b, each later pass
+ * predicts the correction e of A e = r for the start's residual r = b - A p
+ * and adds it (A is linear); every pass is followed by the damped passes.
+ * pfs_session_set_start(s, PFS_START_NETWORK, u) is (coarsen 1, passes 1). */
+int pfs_session_set_start_network(pfs_session *s, pfs_unet *u, int coarsen, int passes);
 
 /* ---- ensembles: many independent simulations in one persistent kernel ------------ */
 /*

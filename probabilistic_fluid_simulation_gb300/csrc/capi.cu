@@ -92,6 +92,7 @@ struct Field {
     pfs::SolveState *dstate = nullptr;  // device
     pfs::SolveState *hstate = nullptr;  // pinned host copy
     float *pback = nullptr;             // plain start kept aside while a predicted start is tried
+    float *pnet = nullptr;              // the network's correction in the later passes of a predicted start
     Reduce red{};
 
     int alloc(int w_, int h_)
@@ -137,6 +138,8 @@ struct Field {
         if (hstate) cudaFreeHost(hstate);
         if (pback) cudaFree(pback);
         pback = nullptr;
+        if (pnet) cudaFree(pnet);
+        pnet = nullptr;
         mem = nullptr;
         rmem = nullptr;
         hres = nullptr;
@@ -162,6 +165,7 @@ struct StepCfg {
     Tuning tun;
     int start_mode = PFS_START_PREVIOUS;
     pfs::unet::Net *net = nullptr;
+    int coarsen = 1, passes = 1;  // predicted start: coarsening of the network's grid, network applications
 };
 
 struct StepOut {
@@ -170,6 +174,7 @@ struct StepOut {
     bool capped = false;
     int start_kind = PFS_START_PREVIOUS;
     double rel_start = -1.0;
+    int start_passes = 0;
 };
 
 bool fused_ok(const Field &f) { return f.w % 4 == 0; }
@@ -334,15 +339,32 @@ int velocity_phase(Field &f, int vp, int tmp, const StepCfg &c, StepOut &o, cuda
         if (!f.pback) CK(cudaMalloc(&f.pback, f.plane * sizeof(float)));
         float *px = f.p[f.pidx[X]];
         CK(cudaMemcpyAsync(f.pback, px, f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
-        CKS(pfs::unet::predict(c.net, f.b, f.ld, px, f.ld, f.h, f.w, st));
+        // damped passes go through the free plane (an even count ends in px)
+        float *scratch = f.p[3 - f.pidx[X] - f.pidx[Y]];
+        o.start_passes = 0;
+        for (int pass = 0; pass < c.passes; ++pass) {
+            if (pass == 0) {
+                CKS(pfs::unet::predict_coarse(c.net, f.b, f.ld, px, f.ld, f.h, f.w, c.coarsen, st));
+            } else {  // correction for the residual: A e = r, added to the start
+                if (!f.pnet) CK(cudaMalloc(&f.pnet, f.plane * sizeof(float)));
+                CK(pfs::launch_residual_field(px, f.b, scratch, f.ld, f.w, f.h, st));
+                CKS(pfs::unet::predict_coarse(c.net, scratch, f.ld, f.pnet, f.ld, f.h, f.w, c.coarsen, st));
+                CK(pfs::launch_add(px, f.pnet, f.plane, st));
+            }
+            for (int k = 0; k < PFS_START_DAMP_PASSES; ++k) {
+                const bool even = (k % 2) == 0;
+                CK(pfs::launch_damp(even ? px : scratch, f.b, even ? scratch : px, f.ld, f.w, f.h, st));
+            }
+            o.start_passes += PFS_START_DAMP_PASSES;
+        }
         double rr, bb;
         CKS(residual_host(f, px, st, rr, bb));
         const double rel_net = relative(rr, bb);
         CKS(residual_host(f, f.pback, st, rr, bb));
         const double rel_plain = relative(rr, bb);
-        if (rel_net < rel_plain) {
+        if (rel_net <= PFS_START_SLACK * rel_plain) {
             o.rel_start = rel_net;
-        } else {  // the prediction is no better than the previous pressure: keep the plain start
+        } else {  // a broken prediction (or not finite): keep the plain start
             CK(cudaMemcpyAsync(px, f.pback, f.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
             o.start_kind = PFS_START_FALLBACK;
             o.rel_start = rel_plain;
@@ -462,6 +484,7 @@ struct pfs_session {
     pfs::LpState *lp = nullptr;  // precision forms other than F32
     int start_mode = PFS_START_PREVIOUS;
     pfs::unet::Net *net = nullptr;
+    int net_coarsen = 1, net_passes = 1;
     ~pfs_session()
     {
         if (img_mem) cudaFree(img_mem);
@@ -646,7 +669,7 @@ static int check_params(const pfs_params *p)
     if (p->fuse_depth < 0 || p->fuse_depth > 8) return fail(PFS_ERR_INVALID_ARGUMENT, "fuse_depth in [0, 8]");
     if (p->chunk_rows < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "chunk_rows must be >= 0");
     if (std::isnan(p->tol)) return fail(PFS_ERR_NOT_FINITE, "tol is NaN");
-    if (p->precision < PFS_PREC_F32 || p->precision > PFS_PREC_F64)
+    if (p->precision < PFS_PREC_F32 || p->precision > PFS_PREC_F32R)
         return fail(PFS_ERR_INVALID_ARGUMENT, "unknown precision form %d", p->precision);
     if (p->precision != PFS_PREC_F32) {
         if (p->viscosity != 0.0f)
@@ -672,6 +695,8 @@ static StepCfg session_cfg(const pfs_session *s)
     if (s->prm.chunk_rows > 0) c.tun.chunk = s->prm.chunk_rows;
     c.start_mode = s->start_mode;
     c.net = s->net;
+    c.coarsen = s->net_coarsen;
+    c.passes = s->net_passes;
     return c;
 }
 
@@ -692,9 +717,10 @@ int pfs_session_create(pfs_session **out, int vx, int vy, int ix, int iy, int iz
     if (!s) return fail(PFS_ERR_CUDA, "out of host memory");
     s->prm = *p;
     s->st = (cudaStream_t)stream;
-    if ((p->precision == PFS_PREC_BF16 || p->precision == PFS_PREC_F16) && vx % 4 != 0) {
+    if ((p->precision == PFS_PREC_BF16 || p->precision == PFS_PREC_F16 || p->precision == PFS_PREC_F32R) &&
+        vx % 4 != 0) {
         delete s;
-        return fail(PFS_ERR_UNSUPPORTED, "16-bit forms need a grid width divisible by 4");
+        return fail(PFS_ERR_UNSUPPORTED, "the refined forms need a grid width divisible by 4");
     }
     if (p->precision != PFS_PREC_F32) {
         int rc = pfs::lp_create(&s->lp, p->precision, vx, vy, iz > 0 ? ix : 0, iz > 0 ? iy : 0, iz);
@@ -809,9 +835,16 @@ int pfs_session_step(pfs_session *s, int n)
         lp.check_every = s->prm.check_every;
         lp.levels = s->prm.fuse_depth > 0 ? s->prm.fuse_depth : 8;
         lp.chunk = s->prm.chunk_rows > 0 ? s->prm.chunk_rows : 32;
+        lp.start_mode = s->start_mode;
+        lp.net = s->net;
+        lp.coarsen = s->net_coarsen;
+        lp.passes = s->net_passes;
         for (int k = 0; k < n; ++k) {
             pfs::LpOut o;
             CKS(pfs::lp_step(s->lp, lp, s->st, o));
+            s->stats.start_kind = o.start_kind;
+            s->stats.rel_start = o.rel_start;
+            s->stats.start_passes = o.start_passes;
             s->stats.sweeps = o.sweeps;
             s->stats.checks = o.checks;
             s->stats.rel_residual = o.rel;
@@ -856,7 +889,25 @@ int pfs_session_step(pfs_session *s, int n)
         s->stats.cap_hits += o.capped ? 1 : 0;
         s->stats.start_kind = o.start_kind;
         s->stats.rel_start = o.rel_start;
+        s->stats.start_passes = o.start_passes;
     }
+    return PFS_OK;
+}
+
+int pfs_session_set_start_network(pfs_session *s, pfs_unet *u, int coarsen, int passes)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    if (!u) return fail(PFS_ERR_INVALID_ARGUMENT, "network start needs a network");
+    if (coarsen < 1 || passes < 1 || passes > 8)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "coarsen must be >= 1 and passes in [1, 8]");
+    if (s->prm.precision == PFS_PREC_F64)
+        return fail(PFS_ERR_UNSUPPORTED, "the F64 form has no network start (the network reads float32 divergence)");
+    if (s->f.w % coarsen || s->f.h % coarsen || (s->f.w / coarsen) % 128 || (s->f.h / coarsen) % 128)
+        return fail(PFS_ERR_UNSUPPORTED, "network start needs grid sides / coarsen that are multiples of 128");
+    s->start_mode = PFS_START_NETWORK;
+    s->net = reinterpret_cast<pfs::unet::Net *>(u);
+    s->net_coarsen = coarsen;
+    s->net_passes = passes;
     return PFS_OK;
 }
 
@@ -865,14 +916,9 @@ int pfs_session_set_start(pfs_session *s, int mode, pfs_unet *u)
     if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
     if (mode < PFS_START_PREVIOUS || mode > PFS_START_NETWORK)
         return fail(PFS_ERR_INVALID_ARGUMENT, "start mode must be PFS_START_PREVIOUS, _ZERO or _NETWORK");
-    if (s->lp) return fail(PFS_ERR_UNSUPPORTED, "start modes apply to float32 sessions");
-    if (mode == PFS_START_NETWORK) {
-        if (!u) return fail(PFS_ERR_INVALID_ARGUMENT, "network start needs a network");
-        if (s->f.w % 128 || s->f.h % 128)
-            return fail(PFS_ERR_UNSUPPORTED, "network start needs grid sides that are multiples of 128");
-    }
+    if (mode == PFS_START_NETWORK) return pfs_session_set_start_network(s, u, 1, 1);
     s->start_mode = mode;
-    s->net = mode == PFS_START_NETWORK ? reinterpret_cast<pfs::unet::Net *>(u) : nullptr;
+    s->net = nullptr;
     return PFS_OK;
 }
 

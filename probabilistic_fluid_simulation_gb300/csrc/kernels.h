@@ -81,6 +81,11 @@ cudaError_t launch_merge_image(float *img, const float *planes, size_t plane, in
 
 // float32 -> float64, n elements (out may be null: nothing to do)
 cudaError_t launch_widen(const float *in, double *out, size_t n, cudaStream_t st);
+// pout = p + (b - A p) / 8 (damped Jacobi pass on a predicted pressure start)
+cudaError_t launch_damp(const float *pin, const float *b, float *pout, int ld, int w, int h, cudaStream_t st);
+// r = b - A p (float, per cell) and p += d: the later passes of a predicted start
+cudaError_t launch_residual_field(const float *p, const float *b, float *r, int ld, int w, int h, cudaStream_t st);
+cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st);
 
 // ---- pressure (sweep_kernels.cu, residual_kernels.cu) ----
 int stream_strip_width(int halo);

@@ -1,6 +1,6 @@
 // Precision forms of the timestep: velocity, image and the pressure
-// correction stored in bf16 / fp16 and computed in FP32, with the pressure
-// itself and its residual kept in FP64 (mixed-precision iterative
+// correction stored in bf16 / fp16 / float32 and computed in FP32, with the
+// pressure itself and its residual kept in FP64 (mixed-precision iterative
 // refinement); and an all-FP64 form, the FP64 run of the same method used to
 // measure every form's error.
 //
@@ -14,8 +14,12 @@
 // r = b - A x, m Jacobi sweeps on A e = r started from e = 0 give
 // x + e = m Jacobi sweeps on A x = b started from x, because a Jacobi sweep is
 // affine (x' = M x + D^-1 b). Only the rounding differs: x, r and the update
-// x += e are FP64; the sweeps on e store e and r in 16 bits (r scaled by
-// 1 / max|r| so it fills the 16-bit range) and compute in FP32.
+// x += e are FP64; the sweeps on e store e and r in 16 or 32 bits (r scaled
+// by 1 / max|r| so it fills the 16-bit range) and compute in FP32.
+//
+// Start of each step's iteration: the previous final pressure (the
+// reference), zero, or the warm-start network's prediction followed by
+// damped passes x += (b - A x) / 8 and checked against the previous pressure.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -27,6 +31,7 @@
 #include "precision.h"
 #include "reduce.cuh"
 #include "storage.cuh"
+#include "unet.h"
 
 namespace pfs {
 namespace {
@@ -224,6 +229,30 @@ __global__ void k_f64_sweep(const double *__restrict__ pin, const double *__rest
     pout[r + i] = __ddiv_rn(__dadd_rn(s, b[r + i]), 4.0);
 }
 
+// Damped Jacobi pass on a predicted start, in FP64: x_out = x + (b - A x) / 8,
+// i.e. the Jacobi update with weight 1/2. Its gain on an error mode of
+// Jacobi eigenvalue l is (1 + l) / 2: zero on the checkerboard mode (l = -1),
+// which undamped sweeps carry unchanged forever, small near it, close to 1 on
+// the smooth modes.
+__global__ void k_lp_damp(const double *__restrict__ x, const float *__restrict__ b, double *__restrict__ xo, int ld,
+                          int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t r = (size_t)j * ld;
+    const double s = __dadd_rn(__dadd_rn(__dadd_rn(x[r + wm_(i, w)], x[r + wp_(i, w)]), x[(size_t)wm_(j, h) * ld + i]),
+                               x[(size_t)wp_(j, h) * ld + i]);
+    const double q = __dsub_rn(__dadd_rn((double)b[r + i], s), __dmul_rn(4.0, x[r + i]));
+    xo[r + i] = __fma_rn(q, 0.125, x[r + i]);
+}
+
+// x += d (a predicted correction), FP64 accumulation.
+__global__ void k_lp_add(double *__restrict__ x, const float *__restrict__ d, size_t n)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        x[k] += (double)d[k];
+}
+
 // FP64 form: residual exactly as the oracle evaluates it, sum r^2 (slot 0).
 __global__ void __launch_bounds__(256) k_f64_residual(const double *__restrict__ p, const double *__restrict__ b,
                                                       int ld, int w, int h, Reduce red)
@@ -329,6 +358,8 @@ struct LpState {
     // b (float, or double in the FP64 form); r (float) and 16-bit r, e x2
     void *u = nullptr, *v = nullptr, *ua = nullptr, *va = nullptr, *img[2] = {nullptr, nullptr};
     double *x[2] = {nullptr, nullptr};
+    double *xback = nullptr;  // the previous pressure, kept while a predicted start is tried
+    float *pred = nullptr;    // the network's pressure (or correction) for a predicted start
     void *b = nullptr;
     float *r = nullptr;
     void *rt = nullptr, *e[2] = {nullptr, nullptr};
@@ -374,9 +405,84 @@ int lp_velocity_and_image(LpState &s, const LpParams &p, cudaStream_t st, double
 
 double rel_of(double rr, double bb) { return bb > 0.0 ? std::sqrt(rr) / std::sqrt(bb) : std::sqrt(rr); }
 
-// One step of a 16-bit form.
+// r = b - A x for the refined forms (no correction): x copied to xo, r to s.r,
+// relative residual returned (blocking).
 template <typename T>
-int lp_step16(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
+int lp_residual(LpState &s, const double *x, double *xo, cudaStream_t st, double &rel)
+{
+    LCK(cudaMemsetAsync(s.maxabs, 0, sizeof(unsigned), st));
+    k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(x, (const T *)nullptr, s.escale, (const float *)s.b, xo, s.r, s.ld,
+                                                   s.w, s.h, s.red, s.maxabs);
+    LCK(launched());
+    LCK(cudaMemcpyAsync(s.hres, s.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    LCK(cudaStreamSynchronize(st));
+    rel = rel_of(s.hres[0], s.hres[1]);
+    return PFS_OK;
+}
+
+// Predicted start: the network's pressure for b (on the grid coarsened
+// p.coarsen times), widened to FP64; then, for each further pass, the
+// network's correction for the residual r = b - A x (A is linear, so the
+// correction solves A e = r as the pressure solves A p = b) added in FP64.
+// Every pass is followed by PFS_START_DAMP_PASSES damped passes. The start is
+// kept unless its residual is above PFS_START_SLACK times the previous
+// pressure's or not finite; then the previous pressure is (PFS_START_FALLBACK). Afterwards x[xcur] holds the start and
+// s.xback the previous pressure.
+template <typename T>
+int lp_network_start(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
+{
+    if (!s.xback) LCK(cudaMalloc(&s.xback, s.plane * sizeof(double)));
+    if (!s.pred) LCK(cudaMalloc(&s.pred, s.plane * sizeof(float)));
+    LCK(cudaMemcpyAsync(s.xback, s.x[s.xcur], s.plane * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    double rel_net = 0.0, rel_plain = 0.0;
+    o.start_passes = 0;
+    for (int pass = 0; pass < p.passes; ++pass) {
+        const float *rhs = pass == 0 ? (const float *)s.b : s.r;  // s.r: residual of x (last lp_residual)
+        const int rc = unet::predict_coarse(p.net, rhs, s.ld, s.pred, s.ld, s.h, s.w, p.coarsen, st);
+        if (rc != PFS_OK) return rc;
+        if (pass == 0) {
+            LCK(launch_widen(s.pred, s.x[s.xcur], s.plane, st));
+        } else {
+            k_lp_add<<<kReduceBlocks, 256, 0, st>>>(s.x[s.xcur], s.pred, s.plane);
+            LCK(launched());
+        }
+        for (int k = 0; k < PFS_START_DAMP_PASSES; ++k) {
+            k_lp_damp<<<g2(s.w, s.h), dim3(kBX, kBY), 0, st>>>(s.x[s.xcur], (const float *)s.b, s.x[1 - s.xcur],
+                                                                 s.ld, s.w, s.h);
+            LCK(launched());
+            s.xcur = 1 - s.xcur;
+        }
+        o.start_passes += PFS_START_DAMP_PASSES;
+        const int e = lp_residual<T>(s, s.x[s.xcur], s.x[1 - s.xcur], st, rel_net);
+        if (e != PFS_OK) return e;
+    }
+    const int e = lp_residual<T>(s, s.xback, s.x[1 - s.xcur], st, rel_plain);  // other slot: previous
+    if (e != PFS_OK) return e;
+    if (rel_net <= PFS_START_SLACK * rel_plain) {
+        o.start_kind = PFS_START_NETWORK;
+        o.rel_start = rel_net;
+    } else {  // a broken prediction (or not finite): keep the plain start
+        s.xcur = 1 - s.xcur;
+        o.start_kind = PFS_START_FALLBACK;
+        o.rel_start = rel_plain;
+    }
+    return PFS_OK;
+}
+
+template <typename T>
+cudaError_t lp_sweeps(const T *in, const T *rhs, T *out, int ld, int w, int h, int L, int chunk, cudaStream_t st)
+{
+    if constexpr (std::is_same<T, __nv_bfloat16>::value)
+        return launch_sweep_stream_bf16(in, rhs, out, ld, w, h, L, chunk, st);
+    else if constexpr (std::is_same<T, __half>::value)
+        return launch_sweep_stream_f16(in, rhs, out, ld, w, h, L, chunk, st);
+    else
+        return launch_sweep_stream(in, rhs, out, nullptr, ld, w, h, L, 8, chunk, nullptr, st);
+}
+
+// One step of a refined form (bf16, fp16 or float32 storage).
+template <typename T>
+int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
 {
     const int w = s.w, h = s.h, ld = s.ld;
     k_lp_advect<T, float><<<g2(w, h), dim3(kBX, kBY), 0, st>>>((T *)s.u, (T *)s.v, (T *)s.ua, (T *)s.va, ld, w, h,
@@ -386,7 +492,18 @@ int lp_step16(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
     k_lp_divergence<T, float, float><<<s.red.nblocks, 256, 0, st>>>((T *)s.ua, (T *)s.va, (float *)s.b, ld, w, h,
                                                                     gamma, s.red);
     LCK(launched());
+    o.start_kind = p.start_mode;
+    if (p.start_mode == PFS_START_ZERO) {
+        LCK(cudaMemsetAsync(s.x[s.xcur], 0, s.plane * sizeof(double), st));
+    } else if (p.start_mode == PFS_START_NETWORK) {
+        const int rc = lp_network_start<T>(s, p, st, o);
+        if (rc != PFS_OK) return rc;
+    }
     const int m = p.check_every > 0 ? p.check_every : 32;  // sweeps between refinements
+    const bool resid = p.tol > 0.0;
+    // predicted start: if the residual stops falling between refinements, the previous pressure takes over
+    const bool watch = resid && o.start_kind == PFS_START_NETWORK;
+    double last_rel = o.rel_start;
     int S = 0;
     T *ecur = nullptr;  // correction of the last inner solve (null before the first)
     o.checks = 0;
@@ -402,9 +519,15 @@ int lp_step16(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
         o.checks++;
         o.rel = rel_of(s.hres[0], s.hres[1]);
         o.bnorm = std::sqrt(s.hres[1]);
-        const bool resid = p.tol > 0.0;
         if ((resid && o.rel <= p.tol) || S >= p.max_iters) break;
-        // inner solve: n sweeps on A e = r from e = 0, 16-bit storage
+        if (watch && ecur && o.start_kind == PFS_START_NETWORK && !(o.rel < last_rel)) {
+            LCK(cudaMemcpyAsync(s.x[s.xcur], s.xback, s.plane * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            o.start_kind = PFS_START_FALLBACK;
+            ecur = nullptr;  // next pass: residual of the previous pressure, no correction
+            continue;
+        }
+        last_rel = o.rel;
+        // inner solve: n sweeps on A e = r from e = 0
         const int n = std::min(m, p.max_iters - S);
         k_lp_scale<T><<<s.red.nblocks, 256, 0, st>>>(s.r, (T *)s.rt, s.plane, s.maxabs, s.escale);
         LCK(launched());
@@ -413,12 +536,7 @@ int lp_step16(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
             const int L = std::min(p.levels, n - done);
             const int out = (cur == 0) ? 1 : 0;
             const T *in = cur < 0 ? nullptr : (const T *)s.e[cur];
-            cudaError_t e;
-            if constexpr (std::is_same<T, __nv_bfloat16>::value)
-                e = launch_sweep_stream_bf16(in, (const T *)s.rt, (T *)s.e[out], ld, w, h, L, p.chunk, st);
-            else
-                e = launch_sweep_stream_f16(in, (const T *)s.rt, (T *)s.e[out], ld, w, h, L, p.chunk, st);
-            LCK(e);
+            LCK(lp_sweeps<T>(in, (const T *)s.rt, (T *)s.e[out], ld, w, h, L, p.chunk, st));
             cur = out;
             done += L;
         }
@@ -442,6 +560,8 @@ int lp_step64(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
     k_lp_divergence<double, double, double><<<s.red.nblocks, 256, 0, st>>>((double *)s.ua, (double *)s.va,
                                                                            (double *)s.b, ld, w, h, gamma, s.red);
     LCK(launched());
+    o.start_kind = p.start_mode;
+    if (p.start_mode == PFS_START_ZERO) LCK(cudaMemsetAsync(s.x[s.xcur], 0, s.plane * sizeof(double), st));
     const bool resid = p.tol > 0.0;
     int S = 0;
     o.checks = 0;
@@ -526,7 +646,7 @@ int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
     s->ic = ic;
     s->ild = rup(std::max(iw, 1), 32);
     s->iplane = (size_t)s->ild * ih;
-    s->tbytes = form == PFS_PREC_F64 ? 8 : 2;
+    s->tbytes = form == PFS_PREC_F64 ? 8 : form == PFS_PREC_F32R ? 4 : 2;
     const size_t P = s->plane, TB = s->tbytes;
     const size_t bbytes = (form == PFS_PREC_F64 ? 8 : 4) * P;
     // u v ua va (T) | x x (double) | b | r (float) | rt e e (T) | image x2 (T)
@@ -557,8 +677,10 @@ int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
     s->img[0] = take(TB * s->iplane * ic);
     s->img[1] = take(TB * s->iplane * ic);
     const int nb = kReduceBlocks;
-    e = cudaMalloc(&s->rmem, (2 * nb + 2) * sizeof(double) + 16 + 16);
-    if (e == cudaSuccess) e = cudaMemset(s->rmem, 0, (2 * nb + 2) * sizeof(double) + 32);
+    // partials (2 nb doubles) | result (2) | escale (1) | tickets 0, 1 and maxabs (3 unsigned, padded to 16 B)
+    const size_t rbytes = (2 * nb + 3) * sizeof(double) + 16;
+    e = cudaMalloc(&s->rmem, rbytes);
+    if (e == cudaSuccess) e = cudaMemset(s->rmem, 0, rbytes);
     if (e == cudaSuccess) e = cudaMallocHost(&s->hres, 2 * sizeof(double));
     if (e != cudaSuccess) {
         lp_destroy(s);
@@ -566,10 +688,10 @@ int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
     }
     s->red.partials = s->rmem;
     s->red.result = s->rmem + 2 * nb;
-    s->red.ticket = reinterpret_cast<unsigned *>(s->rmem + 2 * nb + 2);
+    s->escale = s->rmem + 2 * nb + 2;
+    s->red.ticket = reinterpret_cast<unsigned *>(s->rmem + 2 * nb + 3);
     s->red.nblocks = nb;
     s->maxabs = s->red.ticket + 2;
-    s->escale = reinterpret_cast<double *>(s->rmem + 2 * nb + 2) + 1;
     *out = s;
     return PFS_OK;
 }
@@ -581,6 +703,8 @@ void lp_destroy(LpState *s)
     if (s->rmem) cudaFree(s->rmem);
     if (s->hres) cudaFreeHost(s->hres);
     if (s->stage) cudaFree(s->stage);
+    if (s->xback) cudaFree(s->xback);
+    if (s->pred) cudaFree(s->pred);
     delete s;
 }
 
@@ -590,6 +714,7 @@ int lp_upload(LpState *s, const float *vp_dev, const float *tmp_dev, const float
     case PFS_PREC_BF16: return lp_upload_t<__nv_bfloat16>(*s, vp_dev, tmp_dev, img_dev, st);
     case PFS_PREC_F16: return lp_upload_t<__half>(*s, vp_dev, tmp_dev, img_dev, st);
     case PFS_PREC_F64: return lp_upload_t<double>(*s, vp_dev, tmp_dev, img_dev, st);
+    case PFS_PREC_F32R: return lp_upload_t<float>(*s, vp_dev, tmp_dev, img_dev, st);
     default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
     }
 }
@@ -597,9 +722,10 @@ int lp_upload(LpState *s, const float *vp_dev, const float *tmp_dev, const float
 int lp_step(LpState *s, const LpParams &p, cudaStream_t st, LpOut &o)
 {
     switch (s->form) {
-    case PFS_PREC_BF16: return lp_step16<__nv_bfloat16>(*s, p, st, o);
-    case PFS_PREC_F16: return lp_step16<__half>(*s, p, st, o);
+    case PFS_PREC_BF16: return lp_step_ir<__nv_bfloat16>(*s, p, st, o);
+    case PFS_PREC_F16: return lp_step_ir<__half>(*s, p, st, o);
     case PFS_PREC_F64: return lp_step64(*s, p, st, o);
+    case PFS_PREC_F32R: return lp_step_ir<float>(*s, p, st, o);
     default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
     }
 }
@@ -610,6 +736,7 @@ int lp_download(LpState *s, float *vp_dev, float *img_dev, cudaStream_t st)
     case PFS_PREC_BF16: return lp_download_t<__nv_bfloat16, float>(*s, vp_dev, img_dev, st);
     case PFS_PREC_F16: return lp_download_t<__half, float>(*s, vp_dev, img_dev, st);
     case PFS_PREC_F64: return lp_download_t<double, float>(*s, vp_dev, img_dev, st);
+    case PFS_PREC_F32R: return lp_download_t<float, float>(*s, vp_dev, img_dev, st);
     default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
     }
 }
@@ -620,6 +747,7 @@ int lp_download_f64(LpState *s, double *vp_dev, double *img_dev, cudaStream_t st
     case PFS_PREC_BF16: return lp_download_t<__nv_bfloat16, double>(*s, vp_dev, img_dev, st);
     case PFS_PREC_F16: return lp_download_t<__half, double>(*s, vp_dev, img_dev, st);
     case PFS_PREC_F64: return lp_download_t<double, double>(*s, vp_dev, img_dev, st);
+    case PFS_PREC_F32R: return lp_download_t<float, double>(*s, vp_dev, img_dev, st);
     default: return lp_fail(PFS_ERR_UNSUPPORTED, "unknown precision form");
     }
 }

@@ -7,6 +7,9 @@
 #include "pfs.h"
 
 namespace pfs {
+namespace unet {
+struct Net;
+}
 
 struct LpState;
 
@@ -14,15 +17,22 @@ struct LpParams {
     float dt;
     int max_iters;    // sweep cap (fixed count when tol <= 0)
     double tol;       // relative residual target (<= 0: fixed count)
-    int check_every;  // sweeps between refinements / checks (0: 32 for the 16-bit forms, only at the cap for FP64)
-    int levels;       // sweeps fused per launch (16-bit forms)
+    int check_every;  // sweeps between refinements / checks (0: 32 for the refined forms, only at the cap for FP64)
+    int levels;       // sweeps fused per launch (refined forms)
     int chunk;        // rows per warp in the fused sweep
+    int start_mode = PFS_START_PREVIOUS;  // PFS_START_PREVIOUS / _ZERO / _NETWORK
+    unet::Net *net = nullptr;             // the network of a PFS_START_NETWORK start
+    int coarsen = 1;                      // network run on the grid coarsened this many times
+    int passes = 1;                       // network applications (later ones on the residual)
 };
 
 struct LpOut {
     int sweeps = 0, checks = 0;
     double rel = -1.0, bnorm = -1.0;
     bool capped = false;
+    int start_kind = PFS_START_PREVIOUS;
+    double rel_start = -1.0;
+    int start_passes = 0;
 };
 
 int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic);

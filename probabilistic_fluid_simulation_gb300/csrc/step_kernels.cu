@@ -231,6 +231,60 @@ cudaError_t launch_widen(const float *in, double *out, size_t n, cudaStream_t st
     return launched();
 }
 
+// Damped Jacobi pass on a predicted start: pout = p + (b - A p) / 8, the
+// Jacobi update with weight 1/2 (gain (1 + l) / 2 on an error mode of Jacobi
+// eigenvalue l: zero on the checkerboard mode that undamped sweeps keep).
+__global__ void k_damp(const float *__restrict__ pin, const float *__restrict__ b, float *__restrict__ pout, int ld,
+                       int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t r = (size_t)j * ld;
+    const int im = i == 0 ? w - 1 : i - 1, ip = i + 1 == w ? 0 : i + 1;
+    const int jm = j == 0 ? h - 1 : j - 1, jp = j + 1 == h ? 0 : j + 1;
+    const float q = fsub(fadd(fadd(fadd(fadd(b[r + i], pin[r + im]), pin[r + ip]), pin[(size_t)jm * ld + i]),
+                              pin[(size_t)jp * ld + i]),
+                         fmul(4.0f, pin[r + i]));
+    pout[r + i] = fadd(pin[r + i], fmul(q, 0.125f));
+}
+
+cudaError_t launch_damp(const float *pin, const float *b, float *pout, int ld, int w, int h, cudaStream_t st)
+{
+    k_damp<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(pin, b, pout, ld, w, h);
+    return launched();
+}
+
+// r = b - A p per cell (the sum order of the Jacobi update), float.
+__global__ void k_residual_field(const float *__restrict__ p, const float *__restrict__ b, float *__restrict__ r, int ld,
+                                 int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t o = (size_t)j * ld;
+    const int im = i == 0 ? w - 1 : i - 1, ip = i + 1 == w ? 0 : i + 1;
+    const int jm = j == 0 ? h - 1 : j - 1, jp = j + 1 == h ? 0 : j + 1;
+    r[o + i] = fsub(fadd(fadd(fadd(fadd(b[o + i], p[o + im]), p[o + ip]), p[(size_t)jm * ld + i]), p[(size_t)jp * ld + i]),
+                    fmul(4.0f, p[o + i]));
+}
+
+cudaError_t launch_residual_field(const float *p, const float *b, float *r, int ld, int w, int h, cudaStream_t st)
+{
+    k_residual_field<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(p, b, r, ld, w, h);
+    return launched();
+}
+
+__global__ void k_add(float *__restrict__ p, const float *__restrict__ d, size_t n)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+        p[k] = fadd(p[k], d[k]);
+}
+
+cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
+{
+    k_add<<<kReduceBlocks, 256, 0, st>>>(p, d, n);
+    return launched();
+}
+
 cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h, float dt,
                           cudaStream_t st)
 {

@@ -63,6 +63,7 @@ struct Net {
     float *dD3, *dT2, *dCat3, *dA2, *dX2;
     float *dE4, *dA3, *dX3;
     float *scal = nullptr;  // [0] loss, [1] rms, [2] 1.0
+    float *coarse = nullptr;  // coarse-grid prediction: restricted b, then the coarse pressure (2 x max_pix)
 };
 
 int create(Net **out, int max_pixels)
@@ -180,6 +181,7 @@ void destroy(Net *n)
     cudaFree(n->wmem);
     cudaFree(n->amem);
     cudaFree(n->fmem);
+    if (n->coarse) cudaFree(n->coarse);
     delete n;
 }
 
@@ -336,6 +338,24 @@ int predict(Net *n, const float *b, int ldb, float *p_out, int ldp, int H, int W
     const int rc = forward(n, 1, H, W, st);
     if (rc != PFS_OK) return rc;
     UCK(from_output(n->out, n->scal + 1, p_out, ldp, H, W, st));
+    return PFS_OK;
+}
+
+int predict_coarse(Net *n, const float *b, int ldb, float *p_out, int ldp, int H, int W, int k, cudaStream_t st)
+{
+    if (k == 1) return predict(n, b, ldb, p_out, ldp, H, W, st);
+    if (k < 1 || H % k || W % k)
+        return record_error(PFS_ERR_INVALID_ARGUMENT, "the coarsening factor must divide the grid sides");
+    const int Hc = H / k, Wc = W / k;
+    if (Hc % 128 || Wc % 128 || (size_t)Hc * Wc > n->max_pix)
+        return record_error(PFS_ERR_UNSUPPORTED,
+                            "warm start needs coarse sides that are multiples of 128 within the network's size");
+    if (!n->coarse) UCK(cudaMalloc(&n->coarse, 2 * n->max_pix * sizeof(float)));
+    float *bc = n->coarse, *pc = n->coarse + n->max_pix;
+    UCK(restrict_mean(b, ldb, H, W, k, bc, st));
+    const int rc = predict(n, bc, Wc, pc, Wc, Hc, Wc, st);
+    if (rc != PFS_OK) return rc;
+    UCK(prolong(pc, k, (float)(k * k), p_out, ldp, H, W, st));
     return PFS_OK;
 }
 

@@ -41,6 +41,10 @@ cudaError_t to_input(const float *b, int ld, const float *scale, __nv_bfloat16 *
                      cudaStream_t st);
 cudaError_t from_output(const float *y, const float *scale, float *p, int ld, int H, int W, cudaStream_t st);
 cudaError_t rms(const float *b, int ld, int H, int W, float *out, cudaStream_t st);
+// k x k block means into a dense (H/k) x (W/k) plane; periodic bilinear
+// interpolation of such a plane back to (H, W) times `scale`
+cudaError_t restrict_mean(const float *b, int ld, int H, int W, int k, float *bc, cudaStream_t st);
+cudaError_t prolong(const float *pc, int k, float scale, float *p, int ld, int H, int W, cudaStream_t st);
 
 struct Net;
 int create(Net **out, int max_pixels);
@@ -54,6 +58,11 @@ int forward_backward(Net *n, const float *b, const float *p, int nimg, int H, in
 int adam_step(Net *n, float lr, cudaStream_t st);
 // prediction for one plane: p_out = rms(b) * net(b / rms(b)); planes with row pitch ld
 int predict(Net *n, const float *b, int ldb, float *p_out, int ldp, int H, int W, cudaStream_t st);
+// the same on a grid coarsened k times: b averaged over k x k blocks, the
+// network run at (H/k, W/k), its pressure interpolated back and scaled by k^2
+// (the 5-point operator in cell units scales with the cell size squared);
+// k = 1 is predict()
+int predict_coarse(Net *n, const float *b, int ldb, float *p_out, int ldp, int H, int W, int k, cudaStream_t st);
 
 }  // namespace unet
 }  // namespace pfs

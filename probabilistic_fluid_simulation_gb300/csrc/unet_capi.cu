@@ -62,4 +62,12 @@ int pfs_unet_predict(pfs_unet *u, const float *b, int ldb, float *p, int ldp, in
     return pfs::unet::predict(reinterpret_cast<Net *>(u), b, ldb, p, ldp, h, w, (cudaStream_t)stream);
 }
 
+int pfs_unet_predict_coarse(pfs_unet *u, const float *b, int ldb, float *p, int ldp, int h, int w, int coarsen,
+                            void *stream)
+{
+    if (!u || !b || !p || ldb < w || ldp < w || coarsen < 1)
+        return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad arguments");
+    return pfs::unet::predict_coarse(reinterpret_cast<Net *>(u), b, ldb, p, ldp, h, w, coarsen, (cudaStream_t)stream);
+}
+
 }  // extern "C"

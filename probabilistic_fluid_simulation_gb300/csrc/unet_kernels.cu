@@ -365,6 +365,44 @@ __global__ void __launch_bounds__(1024) k_rms(const float *__restrict__ b, int l
     }
 }
 
+// Coarse-grid prediction. restrict: block means over k x k cells of a plane
+// (pitch ld) into a dense (H/k) x (W/k) plane.
+__global__ void k_restrict(const float *__restrict__ b, int ld, int H, int W, int k, float *__restrict__ bc)
+{
+    const int Wc = W / k, Hc = H / k;
+    const float inv = 1.0f / (float)(k * k);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < Hc * Wc; e += gridDim.x * blockDim.x) {
+        const int I = e % Wc, J = e / Wc;
+        float s = 0.0f;
+        for (int dj = 0; dj < k; ++dj) {
+            const float *row = b + (size_t)(J * k + dj) * ld + I * k;
+            for (int di = 0; di < k; ++di) s += row[di];
+        }
+        bc[e] = s * inv;
+    }
+}
+
+// prolong: periodic bilinear interpolation of a dense (H/k) x (W/k) plane at
+// the fine cell centres, times `scale`, into a plane of pitch ld. Fine cell i
+// sits at coarse coordinate (i + 1/2) / k - 1/2 (coarse cell I's centre is at
+// fine coordinate k I + (k - 1) / 2).
+__global__ void k_prolong(const float *__restrict__ pc, int k, float scale, float *__restrict__ p, int ld, int H, int W)
+{
+    const int Wc = W / k, Hc = H / k;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < H * W; e += gridDim.x * blockDim.x) {
+        const int i = e % W, j = e / W;
+        const float x = ((float)i + 0.5f) / (float)k - 0.5f, y = ((float)j + 0.5f) / (float)k - 0.5f;
+        const float fx = floorf(x), fy = floorf(y);
+        const float sx = x - fx, sy = y - fy;
+        const int i0 = ((int)fx + Wc) % Wc, j0 = ((int)fy + Hc) % Hc;
+        const int i1 = (i0 + 1) % Wc, j1 = (j0 + 1) % Hc;
+        const float v00 = pc[(size_t)j0 * Wc + i0], v10 = pc[(size_t)j0 * Wc + i1];
+        const float v01 = pc[(size_t)j1 * Wc + i0], v11 = pc[(size_t)j1 * Wc + i1];
+        const float v = (1.0f - sy) * ((1.0f - sx) * v00 + sx * v10) + sy * ((1.0f - sx) * v01 + sx * v11);
+        p[(size_t)j * ld + i] = v * scale;
+    }
+}
+
 inline int nblk(size_t n, int t = 256) { return (int)std::min<size_t>((n + t - 1) / t, 152 * 16); }
 
 }  // namespace
@@ -489,6 +527,16 @@ cudaError_t to_input(const float *b, int ld, const float *scale, bf16 *xin, int 
 cudaError_t from_output(const float *y, const float *scale, float *p, int ld, int H, int W, cudaStream_t st)
 {
     k_from_output<<<nblk((size_t)H * W), 256, 0, st>>>(y, scale, p, ld, H, W);
+    return launched();
+}
+cudaError_t restrict_mean(const float *b, int ld, int H, int W, int k, float *bc, cudaStream_t st)
+{
+    k_restrict<<<nblk((size_t)(H / k) * (W / k)), 256, 0, st>>>(b, ld, H, W, k, bc);
+    return launched();
+}
+cudaError_t prolong(const float *pc, int k, float scale, float *p, int ld, int H, int W, cudaStream_t st)
+{
+    k_prolong<<<nblk((size_t)H * W), 256, 0, st>>>(pc, k, scale, p, ld, H, W);
     return launched();
 }
 cudaError_t rms(const float *b, int ld, int H, int W, float *out, cudaStream_t st)

@@ -30,9 +30,10 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "libpfs_gb300.so")
 
 PFS_HOST, PFS_DEVICE = 0, 1
-PREC_F32, PREC_BF16, PREC_F16, PREC_F64 = 0, 1, 2, 3
-PRECISIONS = {"f32": PREC_F32, "bf16": PREC_BF16, "f16": PREC_F16, "f64": PREC_F64}
+PREC_F32, PREC_BF16, PREC_F16, PREC_F64, PREC_F32R = 0, 1, 2, 3, 4
+PRECISIONS = {"f32": PREC_F32, "bf16": PREC_BF16, "f16": PREC_F16, "f64": PREC_F64, "f32r": PREC_F32R}
 START_PREVIOUS, START_ZERO, START_NETWORK, START_FALLBACK = 0, 1, 2, 3
+START_DAMP_PASSES, START_SLACK = 8, 4
 
 
 class PFSError(RuntimeError):
@@ -56,7 +57,8 @@ class Stats(C.Structure):
     """pfs_stats (include/pfs.h)."""
     _fields_ = [("sweeps", C.c_int), ("checks", C.c_int), ("rel_residual", C.c_double), ("bnorm", C.c_double),
                 ("capped", C.c_int), ("steps", C.c_longlong), ("total_sweeps", C.c_longlong),
-                ("cap_hits", C.c_longlong), ("start_kind", C.c_int), ("rel_start", C.c_double)]
+                ("cap_hits", C.c_longlong), ("start_kind", C.c_int), ("rel_start", C.c_double),
+                ("start_passes", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -103,7 +105,10 @@ SIGNATURES = [
     ("pfs_unet_adam_step", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
     ("pfs_unet_predict", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                    C.c_void_p]),
+    ("pfs_unet_predict_coarse", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, C.c_void_p]),
     ("pfs_session_set_start", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    ("pfs_session_set_start_network", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
     ("pfs_ensemble_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
                                       C.POINTER(Params), C.c_void_p]),
     ("pfs_ensemble_upload", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
@@ -284,10 +289,16 @@ class Session:
         _check(lib().pfs_session_stats(self._h, C.byref(s)))
         return s.as_dict()
 
-    def set_start(self, mode: int, net: "UNet" = None):
-        """Initial pressure of each step: START_PREVIOUS (reference), START_ZERO, START_NETWORK."""
+    def set_start(self, mode: int, net: "UNet" = None, coarsen: int = 1, passes: int = 1):
+        """Initial pressure of each step: START_PREVIOUS (reference), START_ZERO,
+        START_NETWORK (the network run on the grid coarsened `coarsen` times,
+        applied `passes` times)."""
         self._net = net  # keep the network alive while the session uses it
-        _check(lib().pfs_session_set_start(self._h, int(mode), net._h if net is not None else None))
+        if mode == START_NETWORK:
+            _check(lib().pfs_session_set_start_network(self._h, net._h if net is not None else None, int(coarsen),
+                                                       int(passes)))
+        else:
+            _check(lib().pfs_session_set_start(self._h, int(mode), net._h if net is not None else None))
 
     def sync(self):
         _check(lib().pfs_session_sync(self._h))
@@ -344,11 +355,16 @@ class UNet:
     def adam_step(self, lr: float, stream: int = 0):
         _check(lib().pfs_unet_adam_step(self._h, float(lr), C.c_void_p(stream or None)))
 
-    def predict(self, b, out, stream: int = 0):
-        """b, out: (h, w) float32 CUDA tensors: out = rms(b) * net(b / rms(b))."""
+    def predict(self, b, out, coarsen: int = 1, stream: int = 0):
+        """b, out: (h, w) float32 CUDA tensors: out = rms(b) * net(b / rms(b)),
+        the network run on the grid coarsened `coarsen` times."""
         h, w = b.shape
-        _check(lib().pfs_unet_predict(self._h, C.c_void_p(_ptr(b)), w, C.c_void_p(_ptr(out)), w, h, w,
-                                      C.c_void_p(stream or None)))
+        if coarsen == 1:
+            _check(lib().pfs_unet_predict(self._h, C.c_void_p(_ptr(b)), w, C.c_void_p(_ptr(out)), w, h, w,
+                                          C.c_void_p(stream or None)))
+        else:
+            _check(lib().pfs_unet_predict_coarse(self._h, C.c_void_p(_ptr(b)), w, C.c_void_p(_ptr(out)), w, h, w,
+                                                 int(coarsen), C.c_void_p(stream or None)))
         return out
 
     def close(self):

@@ -1,0 +1,237 @@
+"""Start modes of the pressure iteration and the refined float32 form.
+
+- PFS_PREC_F32R (float32 sweeps, FP64 pressure and residual) against the FP64
+  form: the same iteration with different rounding;
+- at 256x256 the float32 form stalls above a relative residual of 1e-5 (its
+  rounding floor) while the refined form reaches it in the sweeps the FP64
+  form needs;
+- PFS_START_ZERO in the float32 form is the reference's step with the
+  pressure of both buffers zeroed first (bit-exact against the oracle);
+- PFS_START_NETWORK: a broken prediction (residual not finite or above
+  PFS_START_SLACK times the previous pressure's) is dropped, and the step is
+  then bit-identical to the reference's previous-pressure start; damped
+  passes are counted."""
+import numpy as np
+import pytest
+
+from probabilistic_fluid_simulation_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+F32_DT = float(np.float32(0.1))
+
+
+def run(pfs_lib, form, vp, tmp, steps, *, start=None, net=None, img=None, **kw):
+    h, w, _ = vp.shape
+    with pfs_lib.Session(w, h, image_shape=img.shape if img is not None else None,
+                         precision=pfs_lib.PRECISIONS[form], **kw) as s:
+        if start is not None:
+            s.set_start(start, net)
+        s.upload(vp, tmp, img)
+        sts = []
+        for _ in range(steps):
+            s.step(1)
+            sts.append(s.stats())
+        a = np.empty(vp.shape, np.float64)
+        c = np.empty(img.shape, np.float64) if img is not None else None
+        s.download_f64(a, c)
+    return a, c, sts
+
+
+def rel_err(x, ref):
+    return float(np.abs(x - ref).max() / max(np.abs(ref).max(), 1e-300))
+
+
+def test_f32r_form_tracks_fp64(cuda_device, pfs_lib):
+    """Fixed 200 sweeps, refinement every 50: velocity and image within 1e-5 of
+    the FP64 form after 3 steps (measured 9e-6: float32 storage rounding).
+    Divergence and pressure are held looser (measured 5e-2 and 3e-3): this
+    field is nearly divergence-free, so b is a cancelling difference of
+    float32 velocities whose rounding is a visible part of it."""
+    vp, tmp, img, _ = S.initial_state(256, 192, 3, seed=5)
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=200, check_every=50)
+    ref, ref_i, _ = run(pfs_lib, "f64", vp, tmp, 3, img=img, **kw)
+    got, got_i, sts = run(pfs_lib, "f32r", vp, tmp, 3, img=img, **kw)
+    errs = {k: rel_err(got[..., c], ref[..., c]) for k, c in (("u", 0), ("v", 1), ("p", 2), ("b", 3))}
+    errs["image"] = rel_err(got_i, ref_i)
+    print(errs)
+    assert errs["u"] < 1e-5 and errs["v"] < 1e-5 and errs["image"] < 1e-5, errs
+    assert errs["p"] < 1e-2 and errs["b"] < 0.2, errs
+    assert [s["sweeps"] for s in sts] == [200] * 3
+
+
+def test_f32r_reaches_1e5_where_float32_stalls(cuda_device, pfs_lib):
+    vp, tmp, _, _ = S.initial_state(256, 256, 3, seed=0)
+    kw = dict(dt=0.1, diffuse_iters=2, tol=1e-5, check_every=500)
+    _, _, f32 = run(pfs_lib, "f32", vp, tmp, 1, max_iters=60_000, **kw)
+    _, _, f32r = run(pfs_lib, "f32r", vp, tmp, 1, max_iters=200_000, **kw)
+    _, _, f64 = run(pfs_lib, "f64", vp, tmp, 1, max_iters=200_000, **kw)
+    print(f32[0], f32r[0], f64[0])
+    assert f32[0]["capped"] and f32[0]["rel_residual"] > 1e-5
+    assert not f32r[0]["capped"] and f32r[0]["rel_residual"] <= 1e-5
+    assert not f64[0]["capped"]
+    assert abs(f32r[0]["sweeps"] - f64[0]["sweeps"]) <= 500
+
+
+def test_zero_start_equals_reference_with_zeroed_pressure(cuda_device, pfs_lib, oracle_mod):
+    vp, tmp, _, _ = S.initial_state(64, 48, 3, seed=7)
+    tmp[..., 2] = 0.25  # a nonzero previous pressure that the zero start must ignore
+    vp[..., 2] = -0.5
+    v, t = vp.copy(), tmp.copy()
+    for _ in range(3):
+        v[..., 2] = 0.0
+        t[..., 2] = 0.0
+        v, t, _ = oracle_mod.step(v, t, F32_DT, 0.0, diffuse_iters=2, max_iters=40)
+    h, w, _ = vp.shape
+    with pfs_lib.Session(w, h, dt=F32_DT, diffuse_iters=2, max_iters=40) as s:
+        s.set_start(pfs_lib.START_ZERO)
+        s.upload(vp, tmp)
+        s.step(3)
+        a, b = np.empty_like(vp), np.empty_like(tmp)
+        s.download(a, b)
+        assert s.stats()["start_kind"] == pfs_lib.START_ZERO
+    assert np.array_equal(a, v) and np.array_equal(b, t)
+
+
+def test_previous_pressure_is_anticorrelated(cuda_device, pfs_lib):
+    """The reference's implicit start (the previous step's pressure) is no warm
+    start for this method: the projection subtracts (p_R - p_L) dt / 2 while
+    the divergence takes (u_R - u_L) / -dt, so the next divergence is about
+    b - 2b = -b and consecutive pressures are anti-correlated (measured -0.97
+    on the FP64 oracle). Step 1 starts from the uploaded zero pressure, where
+    both starts coincide."""
+    vp, tmp, _, _ = S.initial_state(64, 64, 3, seed=3)
+    kw = dict(dt=0.1, diffuse_iters=2, tol=1e-5, max_iters=100_000, check_every=50)
+    with pfs_lib.Session(64, 64, precision=pfs_lib.PREC_F32R, **kw) as s:
+        s.upload(vp, tmp)
+        ps, sweeps = [], []
+        for _ in range(3):
+            s.step(1)
+            a = np.empty(vp.shape, np.float64)
+            s.download_f64(a)
+            ps.append(a[..., 2] - a[..., 2].mean())
+            sweeps.append(s.stats()["sweeps"])
+    _, _, zero = run(pfs_lib, "f32r", vp, tmp, 1, start=pfs_lib.START_ZERO, **kw)
+    assert sweeps[0] == zero[0]["sweeps"]
+    for a, b in zip(ps, ps[1:]):
+        assert np.corrcoef(a.ravel(), b.ravel())[0, 1] < -0.9
+
+
+def garbage_net(pfs_lib, pixels):
+    net = pfs_lib.UNet(pixels)
+    rng = np.random.default_rng(0)
+    net.set_params((rng.standard_normal(net.n_params) * 50.0).astype(np.float32))
+    return net
+
+
+@pytest.mark.parametrize("form", ["f32", "f32r"])
+def test_network_start_falls_back_to_the_reference_start(cuda_device, pfs_lib, form):
+    """A network with random weights predicts a pressure whose residual is far
+    above the previous pressure's: every step falls back, and the fields are
+    bit-identical to the previous-pressure start."""
+    vp, tmp, img, _ = S.initial_state(128, 128, 3, seed=9)
+    kw = dict(dt=0.1, diffuse_iters=2, tol=1e-4, max_iters=20_000, check_every=100)
+    net = garbage_net(pfs_lib, 128 * 128)
+    ref, ref_i, ref_s = run(pfs_lib, form, vp, tmp, 3, img=img, **kw)
+    got, got_i, got_s = run(pfs_lib, form, vp, tmp, 3, img=img, start=pfs_lib.START_NETWORK, net=net, **kw)
+    assert [s["start_kind"] for s in got_s] == [pfs_lib.START_FALLBACK] * 3
+    assert [s["start_passes"] for s in got_s] == [pfs_lib.START_DAMP_PASSES] * 3
+    assert [s["sweeps"] for s in got_s] == [s["sweeps"] for s in ref_s]
+    assert np.array_equal(got, ref) and np.array_equal(got_i, ref_i)
+
+
+@pytest.mark.parametrize("form", ["f32", "f32r"])
+def test_network_start_with_zero_network_is_damped_zero_start(cuda_device, pfs_lib, form):
+    """All-zero weights predict p = 0; the damped passes then lower the
+    residual below the zero start's (1.0), so the predicted start is taken."""
+    vp, tmp, _, _ = S.initial_state(128, 128, 3, seed=2)
+    net = pfs_lib.UNet(128 * 128)
+    net.set_params(np.zeros(net.n_params, np.float32))
+    kw = dict(dt=0.1, diffuse_iters=2, tol=1e-4, max_iters=40_000, check_every=100)
+    _, _, sts = run(pfs_lib, form, vp, tmp, 1, start=pfs_lib.START_NETWORK, net=net, **kw)
+    st = sts[0]
+    assert st["start_kind"] == pfs_lib.START_NETWORK and st["start_passes"] == pfs_lib.START_DAMP_PASSES
+    assert 0.0 < st["rel_start"] < 1.0
+    assert st["rel_residual"] <= 1e-4 and not st["capped"]
+
+
+def test_network_start_rejected_where_unsupported(cuda_device, pfs_lib):
+    net = pfs_lib.UNet(128 * 128)
+    with pfs_lib.Session(128, 128, precision=pfs_lib.PREC_F64, diffuse_iters=2) as s:
+        with pytest.raises(pfs_lib.PFSError):
+            s.set_start(pfs_lib.START_NETWORK, net)
+        s.set_start(pfs_lib.START_ZERO)
+    with pfs_lib.Session(96, 96) as s:
+        with pytest.raises(pfs_lib.PFSError):
+            s.set_start(pfs_lib.START_NETWORK, net)
+
+
+def test_coarse_prediction_is_restrict_predict_prolong(cuda_device, pfs_lib):
+    """pfs_unet_predict_coarse = block means (float32, row-major sum order),
+    the network on the coarse grid, periodic bilinear interpolation back to the
+    fine cell centres, times coarsen^2."""
+    import torch
+    k, H, W = 2, 256, 512
+    rng = np.random.default_rng(4)
+    b = rng.standard_normal((H, W)).astype(np.float32)
+    net = pfs_lib.UNet(2 * 128 * 128)
+    net.set_params((rng.standard_normal(net.n_params) * 0.05).astype(np.float32))
+    got = net.predict(torch.from_numpy(b).cuda(), torch.empty(H, W, device="cuda"), coarsen=k).cpu().numpy()
+
+    blocks = b.reshape(H // k, k, W // k, k).transpose(0, 2, 1, 3).reshape(H // k, W // k, k * k)
+    bc = np.zeros((H // k, W // k), np.float32)
+    for t in range(k * k):
+        bc = (bc + blocks[..., t]).astype(np.float32)
+    bc = (bc * np.float32(1.0 / (k * k))).astype(np.float32)
+    pc = net.predict(torch.from_numpy(bc).cuda(), torch.empty(H // k, W // k, device="cuda")).cpu().numpy()
+    pc = pc.astype(np.float64)
+    x = (np.arange(W) + 0.5) / k - 0.5
+    y = (np.arange(H) + 0.5) / k - 0.5
+    i0, j0 = np.floor(x).astype(int), np.floor(y).astype(int)
+    sx, sy = x - i0, y - j0
+    i0, j0 = i0 % (W // k), j0 % (H // k)
+    i1, j1 = (i0 + 1) % (W // k), (j0 + 1) % (H // k)
+    sx, sy = sx[None, :], sy[:, None]
+    ref = ((1 - sy) * ((1 - sx) * pc[np.ix_(j0, i0)] + sx * pc[np.ix_(j0, i1)])
+           + sy * ((1 - sx) * pc[np.ix_(j1, i0)] + sx * pc[np.ix_(j1, i1)])) * k * k
+    assert rel_err(got, ref) < 1e-5, rel_err(got, ref)
+
+
+@pytest.mark.parametrize("form", ["f32", "f32r"])
+def test_network_start_passes_and_coarsening_are_checked(cuda_device, pfs_lib, form):
+    """Later passes add the network's correction for the residual; with
+    all-zero weights every pass adds zero and only the damped passes act, so
+    the start equals 2 x 8 damped passes from zero. Grid sides / coarsen must
+    be multiples of 128."""
+    vp, tmp, _, _ = S.initial_state(256, 256, 3, seed=2)
+    kw = dict(dt=0.1, diffuse_iters=2, tol=1e-4, max_iters=200_000, check_every=100)
+    net = pfs_lib.UNet(256 * 256)
+    net.set_params(np.zeros(net.n_params, np.float32))
+    _, _, one = run(pfs_lib, form, vp, tmp, 1, start=pfs_lib.START_NETWORK, net=net, **kw)
+    h, w, _ = vp.shape
+    with pfs_lib.Session(w, h, precision=pfs_lib.PRECISIONS[form], **kw) as s:
+        s.set_start(pfs_lib.START_NETWORK, net, coarsen=2, passes=2)
+        s.upload(vp, tmp)
+        s.step(1)
+        two = s.stats()
+        with pytest.raises(pfs_lib.PFSError):
+            s.set_start(pfs_lib.START_NETWORK, net, coarsen=4, passes=1)  # 64 is not a multiple of 128
+        with pytest.raises(pfs_lib.PFSError):
+            s.set_start(pfs_lib.START_NETWORK, net, coarsen=1, passes=9)
+    assert one[0]["start_passes"] == 8 and two["start_passes"] == 16
+    assert two["start_kind"] == pfs_lib.START_NETWORK
+    assert two["rel_start"] < one[0]["rel_start"] < 1.0
+
+
+def test_trained_network_saves_sweeps_at_256(cuda_device, pfs_lib):
+    """The shipped network (trained at 256x256) against the zero start, both
+    solved to relative residual 1e-5 in the refined float32 form, on states of
+    seeds the training never saw: measured 15.7% fewer sweeps (network applied
+    twice, damped passes counted as sweeps) and 0.85x the wall time."""
+    from probabilistic_fluid_simulation_gb300 import warmstart as WS
+    params, meta = WS.load_default()
+    r = WS.evaluate(params, 256, [0, 1], steps=2, starts=((1, 2),), log=lambda *_: None)
+    n = r["network"]["coarsen1_passes2"]
+    print(r["zero"]["mean_sweeps"], n["mean_sweeps"], n["sweeps_saved"], n["time_ratio"])
+    assert n["fallbacks"] == 0
+    assert n["sweeps_saved"] > 0.08
