@@ -220,7 +220,7 @@ def reference_arm(a, rank):
 
 
 # ---------------------------------------------------------------------------------------------
-# The other forms (precision, batched), each against the plain FP32 path on the same workload
+# The other forms (precision, batched, warm start), each against the plain path on the same workload
 
 def time_session(fluid, vp, tmp, img, steps, stream, **kw):
     import torch
@@ -246,7 +246,8 @@ def precision_forms(a, fluid, synthetic, stream):
     vp, tmp, img, _ = synthetic.initial_state(n, n, a.channels, a.seed)
     kw = dict(dt=a.dt, diffuse_iters=a.diffuse_iters, max_iters=a.cap, tol=a.tol, check_every=a.check_every)
     out = {"workload": f"{n}x{n}, same solver settings as the headline, {a.form_steps} steps"}
-    for name, prec in (("plain_f32", fluid.PREC_F32), ("bf16", fluid.PREC_BF16), ("f16", fluid.PREC_F16)):
+    for name, prec in (("plain_f32", fluid.PREC_F32), ("bf16", fluid.PREC_BF16), ("f16", fluid.PREC_F16),
+                       ("f32r", fluid.PREC_F32R)):
         out[name] = time_session(fluid, vp, tmp, img, a.form_steps, stream, precision=prec, **kw)
     return out
 
@@ -338,6 +339,43 @@ def batched_form(a, fluid, synthetic, stream):
     out["plain_sessions"] = {"value": cells / el, "unit": UNIT, "ms_per_step": el * 1e3,
                              "how": "one pfs_session per member, stepped one after another (1 step each)"}
     out["members_checked_vs_sessions"] = {"members": sample, "max_abs_diff": maxdiff}
+    return out
+
+
+def warm_start_form(a, fluid, stream):
+    """The learned warm start (shipped network, trained at 256x256): one step
+    to relative residual 1e-5 from zero pressure, network start against zero
+    start, in the refined float32 form (float32 sweeps, FP64 pressure and
+    residual: the float32 pressure cannot represent these solutions to 1e-5).
+    Wall time per step includes the network's inference and damped passes."""
+    from probabilistic_fluid_simulation_gb300 import warmstart as WS
+    params, meta = WS.load_default()
+    out = {"workload": "states of 8-vortex fields (seeds 0, 1; steps 1, 2; dt 0.1) at 256x256 and 1024x1024, "
+                       "one step each from zero pressure to relative residual 1e-5, PFS_PREC_F32R",
+           "network": {"trained_on": f"{meta['pairs']} solver pairs at {meta['size']}x{meta['size']}",
+                       "held_out_loss": meta["training"]["val_loss"][-1]}}
+    for size, (coarsen, passes), every in ((256, (1, 2), 200), (1024, (4, 1), 500)):
+        r = WS.evaluate(params, size, [0, 1], steps=2, check_every=every, starts=((coarsen, passes),),
+                        log=lambda *_: None)
+        z, n = r["zero"], r["network"][f"coarsen{coarsen}_passes{passes}"]
+        out[str(size)] = {
+            "zero_start": {"value": z["cell_updates_per_s"], "unit": UNIT, "ms_per_step": z["mean_ms_per_step"],
+                           "sweeps_per_step": z["mean_sweeps"]},
+            "network_start": {"value": n["cell_updates_per_s"], "unit": UNIT, "ms_per_step": n["mean_ms_per_step"],
+                              "sweeps_per_step": n["mean_sweeps"], "coarsen": coarsen, "passes": passes,
+                              "damped_passes": float(np.mean(n["start_passes"])), "fallbacks": n["fallbacks"]},
+            "sweeps_saved": n["sweeps_saved"], "time_ratio": n["time_ratio"],
+            "previous_start_sweeps": r["previous"]["mean_sweeps"]}
+    # the float32 pressure of the plain path stalls above the tolerance at 256x256
+    from probabilistic_fluid_simulation_gb300 import synthetic
+    vp = synthetic.vortex_field(256, 256, 0)
+    with fluid.Session(256, 256, dt=0.1, diffuse_iters=2, max_iters=100_000, tol=1e-5, check_every=500,
+                       stream=stream) as s:
+        s.upload(vp, np.zeros_like(vp))
+        s.step(1)
+        st = s.stats()
+    out["plain_f32_256"] = {"capped": bool(st["capped"]), "sweeps": st["sweeps"],
+                            "final_rel_residual": st["rel_residual"]}
     return out
 
 
@@ -462,7 +500,8 @@ def main():
     forms = None
     if rank == 0 and not a.no_forms:
         forms = {"precision": precision_forms(a, fluid, synthetic, stream),
-                 "batched": batched_form(a, fluid, synthetic, stream)}
+                 "batched": batched_form(a, fluid, synthetic, stream),
+                 "warm_start": warm_start_form(a, fluid, stream)}
 
     cpu = None
     if rank == 0 and not a.no_cpu and a.cpu_steps > 0:

@@ -1,7 +1,8 @@
 """Learned warm start: training data, training, evaluation.
 
     python -m probabilistic_fluid_simulation_gb300.warmstart train --pairs 20000 --epochs 4 --out weights.npz
-    python -m probabilistic_fluid_simulation_gb300.warmstart eval --weights weights.npz --size 1024
+    python -m probabilistic_fluid_simulation_gb300.warmstart eval --weights weights.npz --size 1024 --starts 4x1
+    python -m probabilistic_fluid_simulation_gb300.warmstart export --out unet.bin
 
 Training pairs come from the solver itself: members of the 256x256 workload
 (8 seeded Gaussian vortices, dt 0.1) are stepped by the ensemble solver with
@@ -290,6 +291,9 @@ def main():
     t.add_argument("--eval-steps", type=int, default=3)
     t.add_argument("--eval-sizes", type=int, nargs="*", default=[256])
     t.add_argument("--eval-starts", default="1x1", help="network starts to evaluate: coarsening x passes, ...")
+    x = sub.add_parser("export", help="write the shipped parameters as raw little-endian float32")
+    x.add_argument("--weights", default=DEFAULT_WEIGHTS)
+    x.add_argument("--out", required=True)
     e = sub.add_parser("eval")
     e.add_argument("--weights", required=True)
     e.add_argument("--size", type=int, default=256)
@@ -314,6 +318,10 @@ def main():
             meta[f"eval_{size}"] = r
             save(a.out, params, meta)
             print(json.dumps(summary(r)))
+    elif a.cmd == "export":
+        params, _ = load(a.weights)
+        params.astype("<f4").tofile(a.out)
+        print(f"{params.size} parameters -> {a.out}")
     else:
         params, _ = load(a.weights)
         r = evaluate(params, a.size, list(range(a.seeds)), steps=a.steps, check_every=a.check_every,
