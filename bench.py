@@ -296,6 +296,18 @@ def batched_form(a, fluid, synthetic, stream):
         launches = (fluid.kernel_launches() - l0) / a.ens_steps
         info = ens.info()
         stats = [ens.stats(k) for k in range(len(sizes))]
+        # ensemble statistics of the image over the largest group of members with one grid size
+        from collections import Counter
+        shape = Counter(sizes).most_common(1)[0][0]
+        group = [k for k, sz in enumerate(sizes) if sz == shape]
+        md = torch.empty(shape[1], shape[0], a.channels, device="cuda")
+        vd = torch.empty_like(md)
+        ens.image_stats(group, md, vd)  # warm-up (allocates the member list)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ens.image_stats(group, md, vd)
+        stats_ms = 1e3 * (time.perf_counter() - t0)
+        ens_mean, ens_var = md.cpu().numpy(), vd.cpu().numpy()
         sample = [0, len(sizes) // 3, 2 * len(sizes) // 3, len(sizes) - 1]
         ens_out = {}
         for k in sample:
@@ -339,6 +351,26 @@ def batched_form(a, fluid, synthetic, stream):
     out["plain_sessions"] = {"value": cells / el, "unit": UNIT, "ms_per_step": el * 1e3,
                              "how": "one pfs_session per member, stepped one after another (1 step each)"}
     out["members_checked_vs_sessions"] = {"members": sample, "max_abs_diff": maxdiff}
+    # the same statistics from per-instance plain runs of the group's members
+    imgs = []
+    for k in group:
+        vp, tmp, img = states[k]
+        h, w, _ = vp.shape
+        with fluid.Session(w, h, image_shape=img.shape, stream=stream, **kw) as s:
+            s.upload(vp, tmp, img)
+            s.step(1 + a.ens_steps)
+            imo = np.empty_like(img)
+            s.download(None, None, imo)
+        imgs.append(imo.astype(np.float64))
+    imgs = np.stack(imgs)
+    out["image_statistics"] = {
+        "members": len(group), "grid": list(shape), "ms": stats_ms,
+        "how": "pointwise mean and population variance of the image over the members of the most common grid "
+               "size (pfs_ensemble_image_stats, FP64 accumulation), against numpy over the same members run as "
+               "plain sessions",
+        "max_abs_diff_mean": float(np.abs(ens_mean - imgs.mean(axis=0)).max()),
+        "max_abs_diff_var": float(np.abs(ens_var - imgs.var(axis=0)).max()),
+        "max_var": float(imgs.var(axis=0).max())}
     return out
 
 

@@ -296,6 +296,12 @@ int pfs_ensemble_config(pfs_ensemble *e, int fuse_depth, int chunk_rows);
 int pfs_ensemble_info(pfs_ensemble *e, int *fuse_depth, int *chunk_rows, int *grid_blocks, int *graphs);
 /* restore == 0: copy the whole state aside (device to device); 1: put it back */
 int pfs_ensemble_snapshot(pfs_ensemble *e, int restore);
+/* Ensemble statistics of the image field: for every pixel and channel, the
+ * mean and the population variance (divide by n) over the n listed members,
+ * which must share one grid size; FP64 accumulation in list order, float32
+ * results interleaved (vy, vx, channels), host or device buffers per `where`.
+ * Returns when the results are written. */
+int pfs_ensemble_image_stats(pfs_ensemble *e, const int *members, int n, float *mean, float *var, int where);
 int pfs_ensemble_destroy(pfs_ensemble *e);
 
 /* ---- kernel-level entry points (tests, tuning, benchmarks) ------------------------ */

@@ -275,6 +275,7 @@ struct Ensemble {
     int snap_icur = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool graphs_ok = true;
+    int *dsel = nullptr;  // member list of pfs_ensemble_image_stats (n ints)
 };
 
 namespace {
@@ -549,6 +550,7 @@ int pfs_ensemble_destroy(pfs_ensemble *e)
     cudaFree(E->stage);
     cudaFree(E->snap);
     cudaFree(E->snap_state);
+    cudaFree(E->dsel);
     delete E;
     return PFS_OK;
 }
@@ -583,6 +585,82 @@ static int ens_stage(Ensemble *E, size_t bytes)
     E->stage_bytes = 0;
     if (cudaMalloc(&E->stage, bytes) != cudaSuccess) return pfs::record_error(PFS_ERR_CUDA, "staging allocation");
     E->stage_bytes = bytes;
+    return PFS_OK;
+}
+
+namespace pfs {
+namespace {
+
+// Pointwise ensemble statistics of the image: for each pixel and channel, the
+// mean and the population variance over the listed members (same grid),
+// accumulated in FP64 in list order (deterministic). One thread per pixel;
+// member planes are read coalesced, the outputs are interleaved (h, w, c).
+__global__ void k_image_stats(const Member *__restrict__ mem, const int *__restrict__ sel, int n, int icur, int c,
+                              int w, int h, float *__restrict__ mean, float *__restrict__ var)
+{
+    const int ld = mem[sel[0]].ld;
+    const size_t plane = (size_t)ld * h;
+    const double inv = 1.0 / (double)n;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < w * h; e += gridDim.x * blockDim.x) {
+        const int i = e % w, j = e / w;
+        const size_t o = (size_t)j * ld + i;
+        for (int ch = 0; ch < c; ++ch) {
+            double s = 0.0, s2 = 0.0;
+            for (int k = 0; k < n; ++k) {
+                const double x = (double)mem[sel[k]].img[icur][ch * plane + o];
+                s += x;
+                s2 = fma(x, x, s2);
+            }
+            const double m = s * inv;
+            mean[(size_t)e * c + ch] = (float)m;
+            var[(size_t)e * c + ch] = (float)fmax(fma(-m, m, s2 * inv), 0.0);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace pfs
+
+#define SCK(x)                                                                  \
+    do {                                                                        \
+        cudaError_t e_ = (x);                                                   \
+        if (e_ != cudaSuccess) {                                                \
+            cudaGetLastError();                                                 \
+            return pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(e_));     \
+        }                                                                       \
+    } while (0)
+
+int pfs_ensemble_image_stats(pfs_ensemble *e, const int *members, int n, float *mean, float *var, int where)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || !members || n <= 0 || n > E->n || !mean || !var || (where != PFS_HOST && where != PFS_DEVICE))
+        return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad image statistics arguments");
+    if (E->c == 0) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "the ensemble has no image");
+    for (int k = 0; k < n; ++k) {
+        const int m = members[k];
+        if (m < 0 || m >= E->n) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "member index out of range");
+        if (E->w[m] != E->w[members[0]] || E->h[m] != E->h[members[0]])
+            return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "image statistics need members of one grid size");
+    }
+    const int w = E->w[members[0]], h = E->h[members[0]];
+    const size_t count = (size_t)w * h * E->c;
+    if (!E->dsel) SCK(cudaMalloc(&E->dsel, sizeof(int) * E->n));
+    SCK(cudaMemcpyAsync(E->dsel, members, sizeof(int) * n, cudaMemcpyHostToDevice, E->st));
+    float *M = mean, *V = var;
+    if (where == PFS_HOST) {
+        const int rc = ens_stage(E, 2 * count * sizeof(float));
+        if (rc != PFS_OK) return rc;
+        M = E->stage;
+        V = E->stage + count;
+    }
+    const int blocks = (int)std::min<size_t>(((size_t)w * h + 255) / 256, 152 * 8);
+    pfs::k_image_stats<<<blocks, 256, 0, E->st>>>(E->dmem, E->dsel, n, E->icur, E->c, w, h, M, V);
+    SCK(pfs::launched());
+    if (where == PFS_HOST) {
+        SCK(cudaMemcpyAsync(mean, M, count * sizeof(float), cudaMemcpyDeviceToHost, E->st));
+        SCK(cudaMemcpyAsync(var, V, count * sizeof(float), cudaMemcpyDeviceToHost, E->st));
+    }
+    SCK(cudaStreamSynchronize(E->st));  // also keeps the member list alive until the kernel has read it
     return PFS_OK;
 }
 

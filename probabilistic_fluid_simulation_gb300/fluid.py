@@ -119,6 +119,8 @@ SIGNATURES = [
     ("pfs_ensemble_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(C.c_int)]),
     ("pfs_ensemble_snapshot", C.c_int, [C.c_void_p, C.c_int]),
+    ("pfs_ensemble_image_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p,
+                                           C.c_int]),
     ("pfs_ensemble_destroy", C.c_int, [C.c_void_p]),
     ("pfs_pressure_sweeps", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                       C.c_int, C.c_int, C.c_int, C.c_void_p]),
@@ -408,6 +410,22 @@ class Ensemble:
         _check(lib().pfs_ensemble_download(self._h, k, C.c_void_p(_ptr(vp) if vp is not None else None),
                                            C.c_void_p(_ptr(image) if image is not None else None), where))
         return vp, image
+
+    def image_stats(self, members, mean=None, var=None):
+        """Pointwise mean and population variance of the image over `members`
+        (one grid size): numpy (h, w, channels) float32 arrays by default, or
+        the given numpy / torch CUDA buffers."""
+        members = [int(m) for m in members]
+        w, h = self.sizes[members[0]]
+        if mean is None:
+            mean = np.empty((h, w, self.channels), np.float32)
+        if var is None:
+            var = np.empty_like(mean) if isinstance(mean, np.ndarray) else mean.new_empty(mean.shape)
+        where = PFS_HOST if isinstance(mean, np.ndarray) else PFS_DEVICE
+        sel = (C.c_int * len(members))(*members)
+        _check(lib().pfs_ensemble_image_stats(self._h, sel, len(members), C.c_void_p(_ptr(mean)),
+                                              C.c_void_p(_ptr(var)), where))
+        return mean, var
 
     def stats(self, k: int) -> dict:
         s = Stats()

@@ -97,3 +97,28 @@ def test_ensemble_rejects_unsupported(cuda_device, pfs_lib):
         pfs_lib.Ensemble([(64, 64)], 3, dt=0.1, diffuse_iters=2, max_iters=100)  # cap not a multiple of 8
     with pytest.raises(pfs_lib.PFSError):
         pfs_lib.Ensemble([(66, 64)], 3, dt=0.1, diffuse_iters=2, max_iters=96)  # width not a multiple of 4
+
+
+def test_ensemble_image_statistics_match_sessions(cuda_device, pfs_lib):
+    """Pointwise mean and population variance of the image over the members of
+    one grid size, against the same members run as plain sessions (whose
+    images equal the members' bit for bit) reduced with numpy in float64."""
+    sizes = [(128, 96)] * 6 + [(64, 64), (128, 96), (96, 128)]
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=64, tol=1e-3, check_every=32)
+    states = [member_state(w, h, k) for k, (w, h) in enumerate(sizes)]
+    group = [k for k, s in enumerate(sizes) if s == (128, 96)]
+    with pfs_lib.Ensemble(sizes, 3, **kw) as ens:
+        for k, st in enumerate(states):
+            ens.upload(k, *st)
+        ens.step(3)
+        mean, var = ens.image_stats(group)
+        with pytest.raises(pfs_lib.PFSError):
+            ens.image_stats([0, 6])  # different grid sizes
+        sub_mean, _ = ens.image_stats(group[:1])
+    imgs = np.stack([session_run(pfs_lib, *states[k], 3, **kw)[2] for k in group]).astype(np.float64)
+    ref_mean, ref_var = imgs.mean(axis=0), imgs.var(axis=0)
+    assert mean.shape == (96, 128, 3)
+    assert np.abs(mean - ref_mean).max() <= 1e-6 * max(1.0, np.abs(ref_mean).max())
+    assert np.abs(var - ref_var).max() <= 1e-6 * max(ref_var.max(), 1e-12) + 1e-9
+    assert np.array_equal(sub_mean, imgs[0].astype(np.float32))
+    assert var.max() > 0.0
