@@ -411,6 +411,52 @@ def warm_start_form(a, fluid, stream):
     return out
 
 
+def cli_form(a):
+    """The command-line driver (same argv as the reference's src/main.cpp) on a
+    1024x1024 velocity PNG and image PNG, 20 steps, NUM_JACOBI_ITERS 30: timed
+    only, and writing every step's image as a PNG. Rates from the driver's own
+    "N timesteps took X us" line."""
+    import re
+    import tempfile
+    from probabilistic_fluid_simulation_gb300 import build as B
+    n, steps = 1024, 20
+    cli = B.CLI_BIN
+    if not os.path.exists(cli):
+        return {"unavailable": "driver not built"}
+    yy, xx = np.mgrid[0:n, 0:n].astype(np.float64)
+    out = {"workload": f"{n}x{n} velocity and image PNGs (RGBA, smooth synthetic), {steps} steps, 30 sweeps"}
+    with tempfile.TemporaryDirectory() as d:
+        for name, ph in (("v.png", 0.3), ("i.png", 1.1)):
+            img = np.stack([0.5 + 0.45 * np.sin(2 * np.pi * (k + 1) * xx / n + ph * k) * np.cos(2 * np.pi * yy / n)
+                            for k in range(4)], axis=-1)
+            rgba = np.clip(np.round(img * 255), 0, 255).astype(np.uint8)
+            _write_png(os.path.join(d, name), rgba)
+        for mode, extra in (("timed_only", []), ("png_every_step", [os.path.join(d, "out")])):
+            r = subprocess.run([cli, str(steps), "0.1", "0.0", os.path.join(d, "i.png"), os.path.join(d, "v.png")]
+                               + extra, capture_output=True, text=True, timeout=600)
+            m = re.search(r"(\d+) timesteps took (\d+) us", r.stdout)
+            if r.returncode != 0 or not m:
+                out[mode] = {"failed": (r.stderr or r.stdout)[-300:]}
+                continue
+            us = int(m.group(2))
+            out[mode] = {"value": n * n * steps / (us / 1e6), "unit": UNIT, "ms_per_step": us / 1e3 / steps}
+    return out
+
+
+def _write_png(path, rgba):
+    import ctypes as C
+    from probabilistic_fluid_simulation_gb300 import build as B
+    lib = C.CDLL(B.PNG_LIB)
+    lib.pfs_png_encode.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
+    lib.pfs_png_free.argtypes = [C.c_void_p]
+    p, sz = C.c_void_p(), C.c_size_t()
+    rgba = np.ascontiguousarray(rgba)
+    assert lib.pfs_png_encode(rgba.ctypes.data, rgba.shape[1], rgba.shape[0], C.byref(p), C.byref(sz)) == 0
+    with open(path, "wb") as f:
+        f.write(C.string_at(p, sz.value))
+    lib.pfs_png_free(p)
+
+
 def main():
     a = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -533,7 +579,8 @@ def main():
     if rank == 0 and not a.no_forms:
         forms = {"precision": precision_forms(a, fluid, synthetic, stream),
                  "batched": batched_form(a, fluid, synthetic, stream),
-                 "warm_start": warm_start_form(a, fluid, stream)}
+                 "warm_start": warm_start_form(a, fluid, stream),
+                 "cli": cli_form(a)}
 
     cpu = None
     if rank == 0 and not a.no_cpu and a.cpu_steps > 0:

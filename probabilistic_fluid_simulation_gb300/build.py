@@ -57,6 +57,36 @@ def _compile(src: str, force: bool, verbose: bool) -> str:
     return obj
 
 
+CLI_DIR = os.path.join(PKG, "cli")
+PNG_LIB = os.path.join(PKG, "libpfs_png.so")
+CLI_BIN = os.path.join(PKG, "fluidsim_gb300")
+
+
+def _stale(target: str, deps) -> bool:
+    return not os.path.exists(target) or os.path.getmtime(target) < max(os.path.getmtime(d) for d in deps)
+
+
+def build_cli(force: bool = False) -> str:
+    """The command-line driver (cli/fluidsim.cpp, linked against the library)
+    and the PNG codec as a small shared library for the tests."""
+    gxx = os.environ.get("CXX", "g++")
+    png = [os.path.join(CLI_DIR, "png.cpp")]
+    deps = png + [os.path.join(CLI_DIR, "png.h")]
+    flags = ["-O2", "-std=c++17", "-Wall"]
+    if force or _stale(PNG_LIB, deps):
+        r = subprocess.run([gxx] + flags + ["-fPIC", "-shared"] + png + ["-o", PNG_LIB], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed for the PNG codec:\n{r.stdout}\n{r.stderr}")
+    main = os.path.join(CLI_DIR, "fluidsim.cpp")
+    if force or _stale(CLI_BIN, deps + [main, LIB, os.path.join(INCLUDE, "pfs.h")]):
+        cmd = [gxx] + flags + [main] + png + ["-I", INCLUDE, "-L", PKG, "-lpfs_gb300", "-Wl,-rpath,$ORIGIN",
+                                              "-o", CLI_BIN]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed for the driver:\n{r.stdout}\n{r.stderr}")
+    return CLI_BIN
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJDIR, exist_ok=True)
     srcs = sources()
@@ -67,6 +97,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli(force)
     return LIB
 
 

@@ -1,0 +1,155 @@
+// Command-line driver with the reference's interface (src/main.cpp):
+//
+//   fluidsim_gb300 <n_timesteps> <delta_t> <viscosity> <input_image> <velocity_field> [output_dir]
+//
+// Same arguments, checks and messages (src/main.cpp:40-42,110-126); the same
+// input conversion: PNG samples as RGBA / 255 (includes/utils.hpp:81-83), the
+// velocity field rescaled to v * VP_RANGE - VP_RANGE / 2 with VP_RANGE = 2 on
+// all four channels (src/main.cpp:171-179), the temporary velocity buffer
+// filled with (-1, -1, -1, 1) (src/main.cpp:186-195); the same loop
+// (simulate_fluid_step then advect_color_step, src/main.cpp:219-246) with the
+// image written after every step as <output_dir>/<step>.png, each sample as
+// (byte)(x * 255) (includes/utils.hpp:128-131); without output_dir the run is
+// timed only. The steps run in a session that keeps the state on the GPU
+// (include/pfs.h); NUM_JACOBI_ITERS (includes/fluid.hpp:11) is taken from the
+// environment variable PFS_JACOBI_ITERS (default 30).
+//
+// Differences from the reference, on purpose: the elapsed time is taken after
+// the device has finished (src/main.cpp:247-254 reads the clock before its
+// cudaDeviceSynchronize); a missing output directory is created; a failing
+// read, write or CUDA call ends the run with a message and exit status 1.
+#include <sys/stat.h>
+
+#include <cerrno>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "pfs.h"
+#include "png.h"
+
+namespace {
+
+constexpr double kVpRange = 2.0;
+
+void usage(const char *prog)
+{
+    std::fprintf(stderr, "Usage: %s <n_timesteps> <delta_t> <viscosity> <input_image> <velocity_field> [output_dir]\n",
+                 prog);
+}
+
+int fail_api(const char *what)
+{
+    std::fprintf(stderr, "%s failed: %s\n", what, pfs_last_error());
+    return 1;
+}
+
+std::vector<float> to_float(const pfs::png::Image &img)
+{
+    std::vector<float> x(img.rgba.size());
+    for (size_t i = 0; i < x.size(); ++i) x[i] = (float)((double)(float)img.rgba[i] / 255.0);
+    return x;
+}
+
+uint8_t to_byte(float x)
+{
+    const double v = (double)x * 255.0;
+    if (!(v > 0.0)) return 0;  // (-1, 0] truncates to 0; below that the reference's cast is undefined
+    if (v >= 255.0) return 255;
+    return (uint8_t)v;  // truncation, as the reference's cast
+}
+
+bool make_dir(const std::string &dir)
+{
+    struct stat st;
+    if (stat(dir.c_str(), &st) == 0) return S_ISDIR(st.st_mode);
+    return mkdir(dir.c_str(), 0755) == 0 || errno == EEXIST;
+}
+
+}  // namespace
+
+int main(int argc, char *argv[])
+{
+    if (argc != 6 && argc != 7) {
+        usage(argv[0]);
+        return 1;
+    }
+    const bool write = argc == 7;
+    const int n_timesteps = std::atoi(argv[1]);
+    const float delta_t = (float)std::atof(argv[2]);
+    const float viscosity = (float)std::atof(argv[3]);
+    if (n_timesteps <= 0) {
+        std::fprintf(stderr, "Timesteps must be greater than 0.\n");
+        return 1;
+    }
+    if (delta_t <= 0) {
+        std::fprintf(stderr, "Delta T must be greater than 0.\n");
+        return 1;
+    }
+    int iters = 30;
+    if (const char *e = std::getenv("PFS_JACOBI_ITERS")) iters = std::atoi(e);
+    if (iters < 1) {
+        std::fprintf(stderr, "PFS_JACOBI_ITERS must be at least 1.\n");
+        return 1;
+    }
+
+    pfs::png::Image input, velocity;
+    std::string err;
+    if (!pfs::png::read_file(argv[4], input, err)) {
+        std::fprintf(stderr, "Something went wrong reading the input image... (%s)\n", err.c_str());
+        return 1;
+    }
+    if (!pfs::png::read_file(argv[5], velocity, err)) {
+        std::fprintf(stderr, "Something went wrong reading the initial velocity field... (%s)\n", err.c_str());
+        return 1;
+    }
+    if (write && !make_dir(argv[6])) {
+        std::fprintf(stderr, "Cannot create the output directory %s\n", argv[6]);
+        return 1;
+    }
+
+    std::vector<float> image = to_float(input), vp = to_float(velocity);
+    for (float &v : vp) v = (float)((double)v * kVpRange - kVpRange / 2.0);
+    std::vector<float> vtmp(vp.size());
+    for (size_t i = 0; i < vtmp.size(); ++i) vtmp[i] = (i % 4) == 3 ? 1.0f : -1.0f;
+
+    pfs_params p;
+    pfs_params_default(&p);
+    p.dt = delta_t;
+    p.viscosity = viscosity;
+    p.diffuse_iters = iters;
+    p.max_iters = iters;
+    p.tol = 0.0;
+    pfs_session *s = nullptr;
+    if (pfs_session_create(&s, velocity.width, velocity.height, input.width, input.height, 4, &p, nullptr) != PFS_OK)
+        return fail_api("pfs_session_create");
+    if (pfs_session_upload(s, vp.data(), vtmp.data(), image.data(), PFS_HOST) != PFS_OK)
+        return fail_api("pfs_session_upload");
+
+    std::printf("Simulating [%d x %d] domain for %d timesteps at dt=%g...\n", velocity.height, velocity.width,
+                n_timesteps, (double)delta_t);
+    std::vector<uint8_t> bytes(image.size());
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    for (int i = 0; i < n_timesteps; ++i) {
+        if (pfs_session_step(s, 1) != PFS_OK) return fail_api("pfs_session_step");
+        if (write) {
+            if (pfs_session_download(s, nullptr, nullptr, image.data(), PFS_HOST) != PFS_OK)
+                return fail_api("pfs_session_download");
+            for (size_t k = 0; k < image.size(); ++k) bytes[k] = to_byte(image[k]);
+            const std::string path = std::string(argv[6]) + "/" + std::to_string(i) + ".png";
+            std::printf("[%d] Writing to : %s\n", i, path.c_str());
+            if (!pfs::png::write_file(path, bytes.data(), input.width, input.height, err)) {
+                std::fprintf(stderr, "%s\n", err.c_str());
+                return 1;
+            }
+        }
+    }
+    if (pfs_session_sync(s) != PFS_OK) return fail_api("pfs_session_sync");
+    const auto t1 = std::chrono::high_resolution_clock::now();
+    std::printf("%d timesteps took %lld us.\n", n_timesteps,
+                (long long)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count());
+    pfs_session_destroy(s);
+    return 0;
+}
