@@ -252,6 +252,20 @@ def precision_forms(a, fluid, synthetic, stream):
     return out
 
 
+def boundary_forms(a, fluid, synthetic, stream):
+    """Boundary modes on the headline workload (2048x2048, same solver
+    settings), 10 steps each: periodic (the reference), the reference's clamp
+    mode, walls."""
+    n = a.size
+    vp, tmp, img, _ = synthetic.initial_state(n, n, a.channels, a.seed)
+    kw = dict(dt=a.dt, diffuse_iters=a.diffuse_iters, max_iters=a.cap, tol=a.tol, check_every=a.check_every)
+    out = {"workload": f"{n}x{n}, same solver settings as the headline, 10 steps"}
+    for name, bc in (("periodic", fluid.BOUNDARY_PERIODIC), ("clamp", fluid.BOUNDARY_CLAMP),
+                     ("walls", fluid.BOUNDARY_WALLS)):
+        out[name] = time_session(fluid, vp, tmp, img, 10, stream, boundary=bc, **kw)
+    return out
+
+
 def ensemble_sizes(n, seed):
     from probabilistic_fluid_simulation_gb300 import synthetic
     rng = synthetic.SplitMix64(seed * 7919 + 17)
@@ -580,7 +594,8 @@ def main():
         forms = {"precision": precision_forms(a, fluid, synthetic, stream),
                  "batched": batched_form(a, fluid, synthetic, stream),
                  "warm_start": warm_start_form(a, fluid, stream),
-                 "cli": cli_form(a)}
+                 "cli": cli_form(a),
+                 "boundary": boundary_forms(a, fluid, synthetic, stream)}
 
     cpu = None
     if rank == 0 and not a.no_cpu and a.cpu_steps > 0:

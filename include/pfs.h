@@ -166,7 +166,23 @@ typedef struct {
     int chunk_rows;     /* rows per warp in the fused sweep, 0 = tuned default      */
     int want_residual;  /* fixed mode: also report the final residual              */
     int precision;      /* PFS_PREC_*                                              */
+    int boundary;       /* PFS_BOUNDARY_* (sessions of the F32 form)               */
 } pfs_params;
+
+/* Boundary mode of the advection (velocity and image):
+ *   PFS_BOUNDARY_PERIODIC  the reference's wrapping mode (src/fluid.cpp:47-52,
+ *                          105-106), default; every other operator is
+ *                          periodic in all modes, as in the reference;
+ *   PFS_BOUNDARY_CLAMP     the reference's commented-out clamp mode
+ *                          (src/fluid.cpp:43-45, 100-102): the backtraced
+ *                          coordinate is std::max(0.5f, std::min<float>(n - 1.5, x))
+ *                          instead of wrapped;
+ *   PFS_BOUNDARY_WALLS     clamp, and zero velocity on the boundary cells
+ *                          (first and last row and column) after advection
+ *                          and after projection: fixed zero-velocity walls.
+ * The non-periodic modes need grid sides of at least 2; the drop-in calls and
+ * ensembles are periodic. */
+enum { PFS_BOUNDARY_PERIODIC = 0, PFS_BOUNDARY_CLAMP = 1, PFS_BOUNDARY_WALLS = 2 };
 
 typedef struct {
     int sweeps;          /* pressure sweeps of the last step               */

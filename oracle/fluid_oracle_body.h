@@ -23,6 +23,20 @@ static inline long FN(cell)(int i, int j, int w, int ch) { return ((long)j * w +
  * fmod(fmod(x, n) + n, n), evaluated in REAL. */
 static inline REAL FN(wrap)(REAL x, REAL n) { return FMOD(FMOD(x, n) + n, n); }
 
+/* Boundary modes of the backtrace: 0 periodic (the reference's wrapping
+ * mode); 1 clamp, the reference's commented-out alternative
+ * (src/fluid.cpp:43-45,100-102): std::max(0.5f, std::min<float>(n - 1.5, x)),
+ * after which i0 + 1 stays inside the grid; 2 walls: clamp, and zero velocity
+ * on the boundary cells after advection and after projection. */
+static inline REAL FN(clampc)(REAL x, REAL n)
+{
+    const REAL hi = (REAL)((double)n - 1.5);
+    const REAL m = (x < hi) ? x : hi;     /* std::min<float>(hi, x): x when x < hi */
+    return ((REAL)0.5 < m) ? m : (REAL)0.5; /* std::max(0.5f, m) */
+}
+static inline REAL FN(bound)(REAL x, REAL n, int bc) { return bc ? FN(clampc)(x, n) : FN(wrap)(x, n); }
+static inline int FN(on_edge)(int i, int j, int w, int h) { return i == 0 || j == 0 || i == w - 1 || j == h - 1; }
+
 /* Bilinear weights and sum in the reference's order, src/fluid.cpp:62-66. */
 static inline REAL FN(bilerp)(REAL sx, REAL sy, REAL f00, REAL f10, REAL f01, REAL f11)
 {
@@ -36,17 +50,22 @@ static inline REAL FN(bilerp)(REAL sx, REAL sy, REAL f00, REAL f10, REAL f01, RE
 /* Velocity advection, src/fluid.cpp:24-70: channels 0-1 of `in` are
  * backtraced by dt*u/width cells (S3), wrapped, and bilinearly sampled into
  * channels 0-1 of `out`; channels 2-3 of `out` are untouched. */
-static void FN(advect)(const REAL *in, REAL *out, int w, int h, REAL dt)
+static void FN(advect)(const REAL *in, REAL *out, int w, int h, REAL dt, int bc)
 {
     const REAL fw = (REAL)w, fh = (REAL)h;
     OMP_FOR
     for (int j = 0; j < h; j++) {
         for (int i = 0; i < w; i++) {
             const long c = FN(cell)(i, j, w, 4);
+            if (bc == 2 && FN(on_edge)(i, j, w, h)) {
+                out[c + 0] = 0;
+                out[c + 1] = 0;
+                continue;
+            }
             REAL xp = (REAL)i - dt * in[c + 0] / fw;
             REAL yp = (REAL)j - dt * in[c + 1] / fh;
-            xp = FN(wrap)(xp, fw);
-            yp = FN(wrap)(yp, fh);
+            xp = FN(bound)(xp, fw, bc);
+            yp = FN(bound)(yp, fh, bc);
             const int i0 = (int)xp, j0 = (int)yp;
             const int i1 = (i0 + 1) % w, j1 = (j0 + 1) % h;
             const REAL sx = xp - (REAL)i0, sy = yp - (REAL)j0;
@@ -62,7 +81,7 @@ static void FN(advect)(const REAL *in, REAL *out, int w, int h, REAL dt)
  * the nearest velocity cell (S4), backtraces by (dt/viw)*u/iwidth, wraps and
  * samples all `ic` channels bilinearly. */
 static void FN(advect_color)(const REAL *img, REAL *out, int iw, int ih, int ic,
-                             const REAL *vel, int vw, int vh, REAL dt)
+                             const REAL *vel, int vw, int vh, REAL dt, int bc)
 {
     const REAL fiw = (REAL)iw, fih = (REAL)ih, fvw = (REAL)vw, fvh = (REAL)vh;
     const REAL viw = fvw / fiw, vih = fvh / fih;
@@ -74,8 +93,8 @@ static void FN(advect_color)(const REAL *img, REAL *out, int iw, int ih, int ic,
             const long vc = FN(cell)(vi, vj, vw, 4);
             REAL xp = (REAL)i - (dt / viw) * vel[vc + 0] / fiw;
             REAL yp = (REAL)j - (dt / vih) * vel[vc + 1] / fih;
-            xp = FN(wrap)(xp, fiw);
-            yp = FN(wrap)(yp, fih);
+            xp = FN(bound)(xp, fiw, bc);
+            yp = FN(bound)(yp, fih, bc);
             const int i0 = (int)xp, j0 = (int)yp;
             const int i1 = (i0 + 1) % iw, j1 = (j0 + 1) % ih;
             const REAL sx = xp - (REAL)i0, sy = yp - (REAL)j0;
@@ -183,7 +202,7 @@ static double FN(residual_sq)(const REAL *x, int w, int h, double *bb, double *r
 
 /* Projection, src/fluid.cpp:269-296 (S7): u -= (pR-pL)*dt/2, v -= (pB-pT)*dt/2,
  * reading pressure and velocity from `in`, writing channels 0-1 of `out`. */
-static void FN(project)(const REAL *in, REAL *out, int w, int h, REAL dt)
+static void FN(project)(const REAL *in, REAL *out, int w, int h, REAL dt, int bc)
 {
     OMP_FOR
     for (int j = 0; j < h; j++) {
@@ -199,6 +218,10 @@ static void FN(project)(const REAL *in, REAL *out, int w, int h, REAL dt)
             const long c = FN(cell)(i, j, w, 4);
             out[c + 0] = in[c + 0] - gx;
             out[c + 1] = in[c + 1] - gy;
+            if (bc == 2 && FN(on_edge)(i, j, w, h)) { /* walls: zero velocity on the boundary cells */
+                out[c + 0] = 0;
+                out[c + 1] = 0;
+            }
         }
     }
 }
@@ -219,16 +242,17 @@ static void FN(swap)(REAL **a, REAL **b) { REAL *t = *a; *a = *b; *b = t; }
  * With diffuse_iters == max_iters == NUM_JACOBI_ITERS and tol <= 0 this is
  * src/fluid.cpp:298-310 exactly.
  */
-int FN(pfso_step)(REAL **vp, REAL **tmp, int w, int h, REAL dt, REAL visc,
-                  int diffuse_iters, int max_iters, double tol, int check_every,
-                  int want_residual, pfso_stats *st)
+int FN(pfso_step_bc)(REAL **vp, REAL **tmp, int w, int h, REAL dt, REAL visc,
+                     int diffuse_iters, int max_iters, double tol, int check_every,
+                     int want_residual, int bc, pfso_stats *st)
 {
-    if (w <= 0 || h <= 0 || diffuse_iters < 0 || max_iters < 0) return -1;
+    if (w <= 0 || h <= 0 || diffuse_iters < 0 || max_iters < 0 || bc < 0 || bc > 2) return -1;
+    if (bc && (w < 2 || h < 2)) return -1;
     double *rowbuf = (double *)malloc(sizeof(double) * 2 * (size_t)h);
     if (!rowbuf) return -2;
 
     /* advect(vp, tmp): src/fluid.cpp:300 */
-    FN(advect)(*vp, *tmp, w, h, dt);
+    FN(advect)(*vp, *tmp, w, h, dt, bc);
 
     /* diffuse(tmp, vp): src/fluid.cpp:301,144-195 */
     {
@@ -270,7 +294,7 @@ int FN(pfso_step)(REAL **vp, REAL **tmp, int w, int h, REAL dt, REAL visc,
     }
 
     /* subtractPressureGradient(tmp, vp): src/fluid.cpp:304,269-296 */
-    FN(project)(*tmp, *vp, w, h, dt);
+    FN(project)(*tmp, *vp, w, h, dt, bc);
 
     free(rowbuf);
     if (st) {
@@ -283,18 +307,33 @@ int FN(pfso_step)(REAL **vp, REAL **tmp, int w, int h, REAL dt, REAL visc,
     return 0;
 }
 
-/* advect_color_step, src/fluid.cpp:312-320: advect, then swap image/itmp. */
-int FN(pfso_advect_color_step)(REAL **image, REAL **itmp, int iw, int ih, int ic,
-                               const REAL *vel, int vw, int vh, REAL dt)
+int FN(pfso_step)(REAL **vp, REAL **tmp, int w, int h, REAL dt, REAL visc,
+                  int diffuse_iters, int max_iters, double tol, int check_every,
+                  int want_residual, pfso_stats *st)
 {
-    if (iw <= 0 || ih <= 0 || ic <= 0 || vw <= 0 || vh <= 0) return -1;
-    FN(advect_color)(*image, *itmp, iw, ih, ic, vel, vw, vh, dt);
+    return FN(pfso_step_bc)(vp, tmp, w, h, dt, visc, diffuse_iters, max_iters, tol, check_every, want_residual, 0,
+                            st);
+}
+
+/* advect_color_step, src/fluid.cpp:312-320: advect, then swap image/itmp. */
+int FN(pfso_advect_color_step_bc)(REAL **image, REAL **itmp, int iw, int ih, int ic,
+                                  const REAL *vel, int vw, int vh, REAL dt, int bc)
+{
+    if (iw <= 0 || ih <= 0 || ic <= 0 || vw <= 0 || vh <= 0 || bc < 0 || bc > 2) return -1;
+    if (bc && (iw < 2 || ih < 2)) return -1;
+    FN(advect_color)(*image, *itmp, iw, ih, ic, vel, vw, vh, dt, bc);
     FN(swap)(image, itmp);
     return 0;
 }
 
+int FN(pfso_advect_color_step)(REAL **image, REAL **itmp, int iw, int ih, int ic,
+                               const REAL *vel, int vw, int vh, REAL dt)
+{
+    return FN(pfso_advect_color_step_bc)(image, itmp, iw, ih, ic, vel, vw, vh, dt, 0);
+}
+
 /* Single operators, exposed for unit tests of each stage. */
-void FN(pfso_advect)(const REAL *in, REAL *out, int w, int h, REAL dt) { FN(advect)(in, out, w, h, dt); }
+void FN(pfso_advect)(const REAL *in, REAL *out, int w, int h, REAL dt) { FN(advect)(in, out, w, h, dt, 0); }
 void FN(pfso_pressure_sweep)(const REAL *in, REAL *out, int w, int h) { FN(pressure_sweep)(in, out, w, h); }
 void FN(pfso_divergence)(REAL *x, REAL *y, int w, int h, REAL dt)
 {

@@ -62,9 +62,17 @@ def lib():
             f.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, real, real,
                           C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(_Stats)]
             f.restype = C.c_int
+            f = getattr(L, "pfso_step_bc" + sfx)
+            f.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, real, real,
+                          C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(_Stats)]
+            f.restype = C.c_int
             f = getattr(L, "pfso_advect_color_step" + sfx)
             f.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
                           C.c_void_p, C.c_int, C.c_int, real]
+            f.restype = C.c_int
+            f = getattr(L, "pfso_advect_color_step_bc" + sfx)
+            f.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
+                          C.c_void_p, C.c_int, C.c_int, real, C.c_int]
             f.restype = C.c_int
             getattr(L, "pfso_advect" + sfx).argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, real]
             getattr(L, "pfso_pressure_sweep" + sfx).argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
@@ -107,11 +115,14 @@ def _pick(ptr: int, arrays):
 
 def step(vp: np.ndarray, tmp: np.ndarray, dt: float, viscosity: float, *, diffuse_iters: int,
          max_iters: int, tol: float = 0.0, check_every: int = 0,
-         want_residual: bool = False) -> Tuple[np.ndarray, np.ndarray, StepStats]:
+         want_residual: bool = False, boundary: int = 0) -> Tuple[np.ndarray, np.ndarray, StepStats]:
     """One timestep (src/fluid.cpp:298-310 generalised; see fluid_oracle_body.h).
 
     Mutates both arrays; returns (vp_after, tmp_after, stats) where the
     first two are the input arrays in the roles the pointer swaps left them.
+    boundary: 0 periodic (the reference), 1 clamp (the reference's commented
+    clamp mode, src/fluid.cpp:43-45), 2 walls (clamp + zero velocity on the
+    boundary cells after advection and projection).
     """
     _check(vp, 4)
     _check(tmp, 4)
@@ -122,9 +133,10 @@ def step(vp: np.ndarray, tmp: np.ndarray, dt: float, viscosity: float, *, diffus
     p_vp = C.c_void_p(vp.ctypes.data)
     p_tmp = C.c_void_p(tmp.ctypes.data)
     st = _Stats()
-    rc = getattr(lib(), "pfso_step" + _sfx(vp))(C.byref(p_vp), C.byref(p_tmp), w, h, real(dt), real(viscosity),
-                                                 int(diffuse_iters), int(max_iters), float(tol),
-                                                 int(check_every), int(want_residual), C.byref(st))
+    rc = getattr(lib(), "pfso_step_bc" + _sfx(vp))(C.byref(p_vp), C.byref(p_tmp), w, h, real(dt),
+                                                    real(viscosity), int(diffuse_iters), int(max_iters),
+                                                    float(tol), int(check_every), int(want_residual),
+                                                    int(boundary), C.byref(st))
     if rc != 0:
         raise RuntimeError(f"pfso_step failed: {rc}")
     a = _pick(p_vp.value, (vp, tmp))
@@ -132,8 +144,8 @@ def step(vp: np.ndarray, tmp: np.ndarray, dt: float, viscosity: float, *, diffus
     return a, b, StepStats(st.sweeps, st.checks, st.rel_residual, st.bnorm, bool(st.capped))
 
 
-def advect_color_step(image: np.ndarray, itmp: np.ndarray, vel: np.ndarray, dt: float):
-    """src/fluid.cpp:312-320: returns (image_after, itmp_after)."""
+def advect_color_step(image: np.ndarray, itmp: np.ndarray, vel: np.ndarray, dt: float, boundary: int = 0):
+    """src/fluid.cpp:312-320: returns (image_after, itmp_after); boundary as in step()."""
     _check(image)
     _check(itmp)
     _check(vel, 4)
@@ -142,8 +154,9 @@ def advect_color_step(image: np.ndarray, itmp: np.ndarray, vel: np.ndarray, dt: 
     real = C.c_float if image.dtype == np.float32 else C.c_double
     p_i = C.c_void_p(image.ctypes.data)
     p_t = C.c_void_p(itmp.ctypes.data)
-    rc = getattr(lib(), "pfso_advect_color_step" + _sfx(image))(C.byref(p_i), C.byref(p_t), iw, ih, ic,
-                                                                 C.c_void_p(vel.ctypes.data), vw, vh, real(dt))
+    rc = getattr(lib(), "pfso_advect_color_step_bc" + _sfx(image))(C.byref(p_i), C.byref(p_t), iw, ih, ic,
+                                                                    C.c_void_p(vel.ctypes.data), vw, vh, real(dt),
+                                                                    int(boundary))
     if rc != 0:
         raise RuntimeError(f"pfso_advect_color_step failed: {rc}")
     return _pick(p_i.value, (image, itmp)), _pick(p_t.value, (image, itmp))
@@ -166,16 +179,18 @@ def pressure_sweep(src: np.ndarray, dst: np.ndarray):
 # ----------------------------------------------------------------------------------------------
 # The reference's own src/fluid.cpp (oracle/_ref), where it could be compiled.
 
-def ref_available(iters: int) -> bool:
-    return os.path.exists(os.path.join(REF_DIR, f"libfluidref_it{iters}.so"))
+def ref_available(iters: int, variant: str = "") -> bool:
+    """variant "" is src/fluid.cpp as it is; "_clamp" its commented clamp mode enabled."""
+    return os.path.exists(os.path.join(REF_DIR, f"libfluidref{variant}_it{iters}.so"))
 
 
 _refs = {}
 
 
-def ref_lib(iters: int):
-    if iters not in _refs:
-        path = os.path.join(REF_DIR, f"libfluidref_it{iters}.so")
+def ref_lib(iters: int, variant: str = ""):
+    key = (iters, variant)
+    if key not in _refs:
+        path = os.path.join(REF_DIR, f"libfluidref{variant}_it{iters}.so")
         L = C.CDLL(path)
         L.pfsref_simulate_fluid_step.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int, C.c_int,
                                                  C.c_float, C.c_float]
@@ -183,27 +198,28 @@ def ref_lib(iters: int):
                                                C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_float]
         L.pfsref_num_jacobi_iters.restype = C.c_int
         assert L.pfsref_num_jacobi_iters() == iters
-        _refs[iters] = L
-    return _refs[iters]
+        _refs[key] = L
+    return _refs[key]
 
 
-def ref_step(iters: int, vp: np.ndarray, tmp: np.ndarray, dt: float, viscosity: float):
+def ref_step(iters: int, vp: np.ndarray, tmp: np.ndarray, dt: float, viscosity: float, variant: str = ""):
     """The reference's simulate_fluid_step (includes/fluid.hpp:109) built with
     NUM_JACOBI_ITERS = iters; returns (vp_after, tmp_after)."""
     _check(vp, 4)
     h, w, _ = vp.shape
     p_vp = C.c_void_p(vp.ctypes.data)
     p_tmp = C.c_void_p(tmp.ctypes.data)
-    ref_lib(iters).pfsref_simulate_fluid_step(C.byref(p_vp), C.byref(p_tmp), w, h, C.c_float(dt),
-                                              C.c_float(viscosity))
+    ref_lib(iters, variant).pfsref_simulate_fluid_step(C.byref(p_vp), C.byref(p_tmp), w, h, C.c_float(dt),
+                                                       C.c_float(viscosity))
     return _pick(p_vp.value, (vp, tmp)), _pick(p_tmp.value, (vp, tmp))
 
 
-def ref_advect_color_step(iters: int, image: np.ndarray, itmp: np.ndarray, vel: np.ndarray, dt: float):
+def ref_advect_color_step(iters: int, image: np.ndarray, itmp: np.ndarray, vel: np.ndarray, dt: float,
+                          variant: str = ""):
     ih, iw, ic = image.shape
     vh, vw, _ = vel.shape
     p_i = C.c_void_p(image.ctypes.data)
     p_t = C.c_void_p(itmp.ctypes.data)
-    ref_lib(iters).pfsref_advect_color_step(C.byref(p_i), C.byref(p_t), iw, ih, ic, C.c_void_p(vel.ctypes.data),
-                                            vw, vh, C.c_float(dt))
+    ref_lib(iters, variant).pfsref_advect_color_step(C.byref(p_i), C.byref(p_t), iw, ih, ic,
+                                                     C.c_void_p(vel.ctypes.data), vw, vh, C.c_float(dt))
     return _pick(p_i.value, (image, itmp)), _pick(p_t.value, (image, itmp))

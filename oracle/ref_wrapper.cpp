@@ -15,6 +15,7 @@
  * The reference source path is passed as PFS_REF_SRC (a string literal) and
  * the sweep count as PFS_REF_ITERS by oracle/Makefile.
  */
+#include <algorithm>  // std::max / std::min of the reference's clamp mode (the clamp build only)
 #define NUM_JACOBI_ITERS (PFS_REF_ITERS)
 typedef struct {
     int x;

@@ -166,6 +166,7 @@ struct StepCfg {
     int start_mode = PFS_START_PREVIOUS;
     pfs::unet::Net *net = nullptr;
     int coarsen = 1, passes = 1;  // predicted start: coarsening of the network's grid, network applications
+    int bc = PFS_BOUNDARY_PERIODIC;  // boundary mode of the advection (pfs_params.boundary)
 };
 
 struct StepOut {
@@ -303,7 +304,7 @@ int velocity_phase(Field &f, int vp, int tmp, const StepCfg &c, StepOut &o, cuda
 {
     const int A = vp, B = tmp;
     // advect(vp, tmp): src/fluid.cpp:300
-    CK(pfs::launch_advect(f.u[A], f.v[A], f.u[B], f.v[B], f.ld, f.w, f.h, c.dt, st));
+    CK(pfs::launch_advect(f.u[A], f.v[A], f.u[B], f.v[B], f.ld, f.w, f.h, c.dt, st, c.bc));
 
     // diffuse(tmp, vp): src/fluid.cpp:301. X ends as the reference's vp (it holds
     // the last diffusion iterate), Y as its tmp.
@@ -657,6 +658,7 @@ void pfs_params_default(pfs_params *p)
     p->fuse_depth = 0;
     p->chunk_rows = 0;
     p->want_residual = 0;
+    p->boundary = PFS_BOUNDARY_PERIODIC;
 }
 
 static int check_params(const pfs_params *p)
@@ -669,6 +671,10 @@ static int check_params(const pfs_params *p)
     if (p->fuse_depth < 0 || p->fuse_depth > 8) return fail(PFS_ERR_INVALID_ARGUMENT, "fuse_depth in [0, 8]");
     if (p->chunk_rows < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "chunk_rows must be >= 0");
     if (std::isnan(p->tol)) return fail(PFS_ERR_NOT_FINITE, "tol is NaN");
+    if (p->boundary < PFS_BOUNDARY_PERIODIC || p->boundary > PFS_BOUNDARY_WALLS)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "unknown boundary mode %d", p->boundary);
+    if (p->boundary != PFS_BOUNDARY_PERIODIC && p->precision != PFS_PREC_F32)
+        return fail(PFS_ERR_UNSUPPORTED, "boundary modes other than periodic run in the F32 form");
     if (p->precision < PFS_PREC_F32 || p->precision > PFS_PREC_F32R)
         return fail(PFS_ERR_INVALID_ARGUMENT, "unknown precision form %d", p->precision);
     if (p->precision != PFS_PREC_F32) {
@@ -697,6 +703,7 @@ static StepCfg session_cfg(const pfs_session *s)
     c.net = s->net;
     c.coarsen = s->net_coarsen;
     c.passes = s->net_passes;
+    c.bc = s->prm.boundary;
     return c;
 }
 
@@ -711,6 +718,8 @@ int pfs_session_create(pfs_session **out, int vx, int vy, int ix, int iy, int iz
     CKS(check_params(p));
     CKS(check_dims(vx, vy, 4, p->dt));
     if (iz < 0 || (iz > 0 && (ix <= 0 || iy <= 0))) return fail(PFS_ERR_INVALID_ARGUMENT, "bad image dims");
+    if (p->boundary != PFS_BOUNDARY_PERIODIC && (vx < 2 || vy < 2 || (iz > 0 && (ix < 2 || iy < 2))))
+        return fail(PFS_ERR_INVALID_ARGUMENT, "clamped boundaries need grid sides of at least 2");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PFS_ERR_NO_DEVICE, "no CUDA device");
     pfs_session *s = new (std::nothrow) pfs_session();
@@ -765,6 +774,9 @@ int pfs_session_set_params(pfs_session *s, const pfs_params *params)
     CKS(check_params(params));
     if (params->precision != s->prm.precision)
         return fail(PFS_ERR_INVALID_ARGUMENT, "the precision form is fixed at session creation");
+    if (params->boundary != PFS_BOUNDARY_PERIODIC &&
+        (s->f.w < 2 || s->f.h < 2 || (s->ic > 0 && (s->iw < 2 || s->ih < 2))))
+        return fail(PFS_ERR_INVALID_ARGUMENT, "clamped boundaries need grid sides of at least 2");
     s->prm = *params;
     return PFS_OK;
 }
@@ -866,14 +878,14 @@ int pfs_session_step(pfs_session *s, int n)
         if (s->ic > 0 && s->iw == f.w && s->ih == f.h) {
             float *src = s->img[s->icur], *dst = s->img[1 - s->icur];
             CK(pfs::launch_project_advect_image(f.u[Z], f.v[Z], pz, f.u[W], f.v[W], f.ld, f.w, f.h, c.dt, src, dst,
-                                                s->iplane, s->ic, s->st));
+                                                s->iplane, s->ic, s->st, c.bc));
             s->icur = 1 - s->icur;
         } else {
-            CK(pfs::launch_project(f.u[Z], f.v[Z], pz, f.u[W], f.v[W], f.ld, f.w, f.h, c.dt, s->st));
+            CK(pfs::launch_project(f.u[Z], f.v[Z], pz, f.u[W], f.v[W], f.ld, f.w, f.h, c.dt, s->st, c.bc));
             if (s->ic > 0) {
                 float *src = s->img[s->icur], *dst = s->img[1 - s->icur];
                 CK(pfs::launch_advect_image_planar(src, dst, s->iplane, s->ild, s->iw, s->ih, s->ic, f.u[W], f.v[W],
-                                                   f.ld, f.w, f.h, c.dt, s->st));
+                                                   f.ld, f.w, f.h, c.dt, s->st, c.bc));
                 s->icur = 1 - s->icur;
             }
         }

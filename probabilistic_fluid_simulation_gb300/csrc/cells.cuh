@@ -13,20 +13,43 @@ namespace {
 __device__ __forceinline__ int wm(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wp(int i, int n) { return i + 1 == n ? 0 : i + 1; }
 
-// Backtrace, wrap and corner cells of one sample (src/fluid.cpp:39-58 and
-// :97-114): x' = i - (k*u)/n wrapped to [0, n).
+// Boundary modes of the backtrace (pfs_params.boundary): 0 periodic wrap (the
+// reference); 1 clamp, the reference's commented-out alternative
+// (src/fluid.cpp:43-45,100-102): std::max(0.5f, std::min<float>(n - 1.5, x)),
+// after which i0 + 1 stays inside the grid; 2 walls: clamp, and zero velocity
+// on the boundary cells after advection and after projection.
+template <int BC>
+__device__ __forceinline__ float bound_coord(float x, float n)
+{
+    if constexpr (BC == 0) {
+        return wrap_coord(x, n);
+    } else {
+        const float hi = fsub(n, 1.5f);        // exact: n is an integer below 2^23
+        const float m = (x < hi) ? x : hi;     // std::min<float>(hi, x)
+        return (0.5f < m) ? m : 0.5f;          // std::max(0.5f, m)
+    }
+}
+
+__device__ __forceinline__ bool on_edge(int i, int j, int w, int h)
+{
+    return i == 0 || j == 0 || i == w - 1 || j == h - 1;
+}
+
+// Backtrace, wrap (or clamp) and corner cells of one sample (src/fluid.cpp:39-58
+// and :97-114): x' = i - (k*u)/n wrapped to [0, n).
 struct Corners {
     int i0, i1, j0, j1;
     float sx, sy;
 };
 
+template <int BC = 0>
 __device__ __forceinline__ Corners backtrace(int i, int j, float kx, float ky, float u, float v, float fw, float fh,
                                             int w, int h)
 {
     float xp = fsub((float)i, fdiv(fmul(kx, u), fw));
     float yp = fsub((float)j, fdiv(fmul(ky, v), fh));
-    xp = wrap_coord(xp, fw);
-    yp = wrap_coord(yp, fh);
+    xp = bound_coord<BC>(xp, fw);
+    yp = bound_coord<BC>(yp, fh);
     Corners c;
     c.i0 = cell_of(xp, w);
     c.j0 = cell_of(yp, h);
@@ -38,12 +61,18 @@ __device__ __forceinline__ Corners backtrace(int i, int j, float kx, float ky, f
 }
 
 // Velocity advection of cell (i, j), src/fluid.cpp:24-70.
+template <int BC = 0>
 __device__ __forceinline__ void advect_cell(const float *__restrict__ u, const float *__restrict__ v,
                                             float *__restrict__ uo, float *__restrict__ vo, int ld, int w, int h,
                                             float dt, int i, int j)
 {
     const size_t o = (size_t)j * ld + i;
-    const Corners c = backtrace(i, j, dt, dt, u[o], v[o], (float)w, (float)h, w, h);
+    if (BC == 2 && on_edge(i, j, w, h)) {
+        uo[o] = 0.0f;
+        vo[o] = 0.0f;
+        return;
+    }
+    const Corners c = backtrace<BC>(i, j, dt, dt, u[o], v[o], (float)w, (float)h, w, h);
     const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
     uo[o] = bilerp(c.sx, c.sy, u[r0 + c.i0], u[r0 + c.i1], u[r1 + c.i0], u[r1 + c.i1]);
     vo[o] = bilerp(c.sx, c.sy, v[r0 + c.i0], v[r0 + c.i1], v[r1 + c.i0], v[r1 + c.i1]);
@@ -86,7 +115,9 @@ __device__ __forceinline__ void residual_sq(FFAcc &acc, float b, float l, float 
     acc.add(sq, __fadd_rn(sq_err, cross));
 }
 
-// Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2.
+// Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2
+// (walls: zero on the boundary cells).
+template <int BC = 0>
 __device__ __forceinline__ void project_cell(const float *__restrict__ u, const float *__restrict__ v,
                                              const float *__restrict__ p, int ld, int w, int h, float dt, int i,
                                              int j, float &uo, float &vo)
@@ -96,10 +127,15 @@ __device__ __forceinline__ void project_cell(const float *__restrict__ u, const 
     const float gy = fmul(fmul(fsub(p[(size_t)wp(j, h) * ld + i], p[(size_t)wm(j, h) * ld + i]), dt), 0.5f);
     uo = fsub(u[r + i], gx);
     vo = fsub(v[r + i], gy);
+    if (BC == 2 && on_edge(i, j, w, h)) {
+        uo = 0.0f;
+        vo = 0.0f;
+    }
 }
 
 // Projection then image advection of cell (i, j) with the just-projected
 // velocity (image grid = velocity grid: viw = vih = 1, and dt / viw = dt).
+template <int BC = 0>
 __device__ __forceinline__ void project_image_cell(const float *__restrict__ u, const float *__restrict__ v,
                                                    const float *__restrict__ p, float *__restrict__ uo,
                                                    float *__restrict__ vo, int ld, int w, int h, float dt,
@@ -107,11 +143,11 @@ __device__ __forceinline__ void project_image_cell(const float *__restrict__ u, 
                                                    size_t plane, int c, int i, int j)
 {
     float un, vn;
-    project_cell(u, v, p, ld, w, h, dt, i, j, un, vn);
+    project_cell<BC>(u, v, p, ld, w, h, dt, i, j, un, vn);
     const size_t o = (size_t)j * ld + i;
     uo[o] = un;
     vo[o] = vn;
-    const Corners k = backtrace(i, j, dt, dt, un, vn, (float)w, (float)h, w, h);
+    const Corners k = backtrace<BC>(i, j, dt, dt, un, vn, (float)w, (float)h, w, h);
     const size_t r0 = (size_t)k.j0 * ld, r1 = (size_t)k.j1 * ld;
     for (int ch = 0; ch < c; ++ch) {
         const float *s = img + ch * plane;

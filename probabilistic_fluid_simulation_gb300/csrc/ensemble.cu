@@ -465,7 +465,7 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
     *out = nullptr;
     const pfs_params &p = *params;
     if (!(p.dt > 0.0f) || p.viscosity != 0.0f || p.diffuse_iters < 2 || p.diffuse_iters % 2 ||
-        p.precision != PFS_PREC_F32)
+        p.boundary != PFS_BOUNDARY_PERIODIC || p.precision != PFS_PREC_F32)
         return pfs::record_error(PFS_ERR_UNSUPPORTED,
                                  "ensembles run float32 steps with viscosity 0 and an even diffusion count >= 2");
     const int L = p.fuse_depth > 0 ? p.fuse_depth : 8;

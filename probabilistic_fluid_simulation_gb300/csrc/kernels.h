@@ -48,22 +48,22 @@ struct SolveState {
 
 // ---- velocity / image / layout (step_kernels.cu) ----
 cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h, float dt,
-                          cudaStream_t st);
+                          cudaStream_t st, int bc = 0);
 cudaError_t launch_diffuse_sweep(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h,
                                  float alpha, float beta, cudaStream_t st);
 // b = gamma * ((u[i+1]-u[i-1]) + (v[j+1]-v[j-1])); sum b^2 into red.result[1]
 cudaError_t launch_divergence(const float *u, const float *v, float *b, int ld, int w, int h, float gamma,
                               const Reduce &red, cudaStream_t st);
 cudaError_t launch_project(const float *u, const float *v, const float *p, float *uo, float *vo, int ld, int w,
-                           int h, float dt, cudaStream_t st);
+                           int h, float dt, cudaStream_t st, int bc = 0);
 // projection fused with image advection when the image grid equals the velocity grid
 cudaError_t launch_project_advect_image(const float *u, const float *v, const float *p, float *uo, float *vo,
                                         int ld, int w, int h, float dt, const float *img, float *imgo,
-                                        size_t img_plane, int c, cudaStream_t st);
+                                        size_t img_plane, int c, cudaStream_t st, int bc = 0);
 // image advection, planar image (c planes of img_plane floats, row pitch ild), planar velocity
 cudaError_t launch_advect_image_planar(const float *img, float *imgo, size_t img_plane, int ild, int iw, int ih,
                                        int c, const float *u, const float *v, int vld, int vw, int vh, float dt,
-                                       cudaStream_t st);
+                                       cudaStream_t st, int bc = 0);
 // image advection on the reference's interleaved layout (image HWC with c
 // channels, velocity HWC with 4 channels)
 cudaError_t launch_advect_image_interleaved(const float *img, float *imgo, int iw, int ih, int c,

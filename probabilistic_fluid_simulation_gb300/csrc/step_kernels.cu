@@ -16,13 +16,14 @@ constexpr int kBX = 32, kBY = 8;
 
 inline dim3 grid2d(int w, int h) { return dim3((w + kBX - 1) / kBX, (h + kBY - 1) / kBY); }
 
-// src/fluid.cpp:24-70
+// src/fluid.cpp:24-70 (BC: boundary mode, cells.cuh)
+template <int BC>
 __global__ void k_advect(const float *__restrict__ u, const float *__restrict__ v, float *__restrict__ uo,
                          float *__restrict__ vo, int ld, int w, int h, float dt)
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    advect_cell(u, v, uo, vo, ld, w, h, dt, i, j);
+    advect_cell<BC>(u, v, uo, vo, ld, w, h, dt, i, j);
 }
 
 // One diffusion sweep, src/fluid.cpp:151-186
@@ -111,13 +112,14 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *
     }
 }
 
+template <int BC>
 __global__ void k_project(const float *__restrict__ u, const float *__restrict__ v, const float *__restrict__ p,
                           float *__restrict__ uo, float *__restrict__ vo, int ld, int w, int h, float dt)
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
     float a, c;
-    project_cell(u, v, p, ld, w, h, dt, i, j, a, c);
+    project_cell<BC>(u, v, p, ld, w, h, dt, i, j, a, c);
     uo[(size_t)j * ld + i] = a;
     vo[(size_t)j * ld + i] = c;
 }
@@ -126,6 +128,7 @@ __global__ void k_project(const float *__restrict__ u, const float *__restrict__
 // same cell with the just-projected velocity. Valid when the image grid equals
 // the velocity grid: then viw = vih = 1 and the nearest velocity cell of pixel
 // (i, j) is (i, j) itself.
+template <int BC>
 __global__ void k_project_advect_image(const float *__restrict__ u, const float *__restrict__ v,
                                        const float *__restrict__ p, float *__restrict__ uo, float *__restrict__ vo,
                                        int ld, int w, int h, float dt, const float *__restrict__ img,
@@ -133,10 +136,11 @@ __global__ void k_project_advect_image(const float *__restrict__ u, const float 
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    project_image_cell(u, v, p, uo, vo, ld, w, h, dt, img, imgo, plane, c, i, j);
+    project_image_cell<BC>(u, v, p, uo, vo, ld, w, h, dt, img, imgo, plane, c, i, j);
 }
 
 // Image advection, src/fluid.cpp:72-127, planar image and velocity.
+template <int BC>
 __global__ void k_advect_image_planar(const float *__restrict__ img, float *__restrict__ imgo, size_t plane,
                                       int ild, int iw, int ih, int c, const float *__restrict__ u,
                                       const float *__restrict__ v, int vld, int vw, int vh, float dt, float viw,
@@ -147,7 +151,7 @@ __global__ void k_advect_image_planar(const float *__restrict__ img, float *__re
     const int vi = min(__float2int_rz(fmul((float)i, viw)), vw - 1);
     const int vj = min(__float2int_rz(fmul((float)j, vih)), vh - 1);
     const size_t vo = (size_t)vj * vld + vi;
-    const Corners k = backtrace(i, j, kx, ky, u[vo], v[vo], (float)iw, (float)ih, iw, ih);
+    const Corners k = backtrace<BC>(i, j, kx, ky, u[vo], v[vo], (float)iw, (float)ih, iw, ih);
     const size_t r0 = (size_t)k.j0 * ild, r1 = (size_t)k.j1 * ild, o = (size_t)j * ild + i;
     for (int ch = 0; ch < c; ++ch) {
         const float *s = img + ch * plane;
@@ -285,10 +289,20 @@ cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
     return launched();
 }
 
+#define PFS_BC_DISPATCH(bc, KERNEL, GRID, ...)                                     \
+    do {                                                                           \
+        switch (bc) {                                                              \
+        case 0: KERNEL<0><<<GRID, dim3(kBX, kBY), 0, st>>>(__VA_ARGS__); break;    \
+        case 1: KERNEL<1><<<GRID, dim3(kBX, kBY), 0, st>>>(__VA_ARGS__); break;    \
+        case 2: KERNEL<2><<<GRID, dim3(kBX, kBY), 0, st>>>(__VA_ARGS__); break;    \
+        default: return cudaErrorInvalidValue;                                     \
+        }                                                                          \
+    } while (0)
+
 cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h, float dt,
-                          cudaStream_t st)
+                          cudaStream_t st, int bc)
 {
-    k_advect<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, uo, vo, ld, w, h, dt);
+    PFS_BC_DISPATCH(bc, k_advect, grid2d(w, h), u, v, uo, vo, ld, w, h, dt);
     return launched();
 }
 
@@ -341,18 +355,18 @@ cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, c
 }
 
 cudaError_t launch_project(const float *u, const float *v, const float *p, float *uo, float *vo, int ld, int w,
-                           int h, float dt, cudaStream_t st)
+                           int h, float dt, cudaStream_t st, int bc)
 {
-    k_project<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, p, uo, vo, ld, w, h, dt);
+    PFS_BC_DISPATCH(bc, k_project, grid2d(w, h), u, v, p, uo, vo, ld, w, h, dt);
     return launched();
 }
 
 cudaError_t launch_project_advect_image(const float *u, const float *v, const float *p, float *uo, float *vo,
                                         int ld, int w, int h, float dt, const float *img, float *imgo,
-                                        size_t img_plane, int c, cudaStream_t st)
+                                        size_t img_plane, int c, cudaStream_t st, int bc)
 {
-    k_project_advect_image<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(u, v, p, uo, vo, ld, w, h, dt, img, imgo,
-                                                                     img_plane, c);
+    PFS_BC_DISPATCH(bc, k_project_advect_image, grid2d(w, h), u, v, p, uo, vo, ld, w, h, dt, img, imgo, img_plane,
+                    c);
     return launched();
 }
 
@@ -367,12 +381,12 @@ static void image_scales(int iw, int ih, int vw, int vh, float dt, float &viw, f
 
 cudaError_t launch_advect_image_planar(const float *img, float *imgo, size_t img_plane, int ild, int iw, int ih,
                                        int c, const float *u, const float *v, int vld, int vw, int vh, float dt,
-                                       cudaStream_t st)
+                                       cudaStream_t st, int bc)
 {
     float viw, vih, kx, ky;
     image_scales(iw, ih, vw, vh, dt, viw, vih, kx, ky);
-    k_advect_image_planar<<<grid2d(iw, ih), dim3(kBX, kBY), 0, st>>>(img, imgo, img_plane, ild, iw, ih, c, u, v, vld,
-                                                                     vw, vh, dt, viw, vih, kx, ky);
+    PFS_BC_DISPATCH(bc, k_advect_image_planar, grid2d(iw, ih), img, imgo, img_plane, ild, iw, ih, c, u, v, vld, vw, vh,
+                    dt, viw, vih, kx, ky);
     return launched();
 }
 

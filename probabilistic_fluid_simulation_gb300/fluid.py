@@ -34,6 +34,7 @@ PREC_F32, PREC_BF16, PREC_F16, PREC_F64, PREC_F32R = 0, 1, 2, 3, 4
 PRECISIONS = {"f32": PREC_F32, "bf16": PREC_BF16, "f16": PREC_F16, "f64": PREC_F64, "f32r": PREC_F32R}
 START_PREVIOUS, START_ZERO, START_NETWORK, START_FALLBACK = 0, 1, 2, 3
 START_DAMP_PASSES, START_SLACK = 8, 4
+BOUNDARY_PERIODIC, BOUNDARY_CLAMP, BOUNDARY_WALLS = 0, 1, 2
 
 
 class PFSError(RuntimeError):
@@ -50,7 +51,7 @@ class Params(C.Structure):
     """pfs_params (include/pfs.h)."""
     _fields_ = [("dt", C.c_float), ("viscosity", C.c_float), ("diffuse_iters", C.c_int), ("max_iters", C.c_int),
                 ("tol", C.c_double), ("check_every", C.c_int), ("fuse_depth", C.c_int), ("chunk_rows", C.c_int),
-                ("want_residual", C.c_int), ("precision", C.c_int)]
+                ("want_residual", C.c_int), ("precision", C.c_int), ("boundary", C.c_int)]
 
 
 class Stats(C.Structure):

@@ -16,6 +16,8 @@ with channels 0-2 set to 1, src/test/test_pressure.cpp:9-37,52-75, and the
 vortex fields covering even and odd sweep counts, viscosity, rectangular
 grids, an image whose resolution differs from the velocity grid, and
 non-zero initial pressure in both buffers (the implicit warm start).
+golden/clamp/ holds two cases of the reference's clamp mode (its commented
+clamp lines enabled by oracle/Makefile).
 The 256x256 / 40-sweep / 100-step workload is stored as SHA-256 digests of
 the final buffers.
 """
@@ -37,19 +39,19 @@ from probabilistic_fluid_simulation_gb300 import synthetic as S  # noqa: E402
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
-def run_ref(iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps):
+def run_ref(iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps, variant=""):
     vp, tmp, img, itmp = vp.copy(), tmp.copy(), img.copy(), itmp.copy()
     snaps = {}
     for s in range(1, steps + 1):
-        vp, tmp = O.ref_step(iters, vp, tmp, dt, visc)
-        img, itmp = O.ref_advect_color_step(iters, img, itmp, vp, dt)
+        vp, tmp = O.ref_step(iters, vp, tmp, dt, visc, variant)
+        img, itmp = O.ref_advect_color_step(iters, img, itmp, vp, dt, variant)
         if s in snap_steps:
             snaps[s] = (vp.copy(), tmp.copy(), img.copy(), itmp.copy())
     return snaps
 
 
-def save_case(name, iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps):
-    snaps = run_ref(iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps)
+def save_case(name, iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps, variant="", out=OUT):
+    snaps = run_ref(iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps, variant)
     arrays = dict(in_vp=vp, in_tmp=tmp, in_img=img, in_itmp=itmp)
     for s, (a, b, c, d) in snaps.items():
         arrays[f"vp_s{s}"] = a
@@ -57,7 +59,10 @@ def save_case(name, iters, vp, tmp, img, itmp, dt, visc, steps, snap_steps):
         arrays[f"img_s{s}"] = c
         arrays[f"itmp_s{s}"] = d
     meta = dict(iters=iters, dt=dt, viscosity=visc, steps=steps, snaps=sorted(snaps))
-    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), meta=json.dumps(meta), **arrays)
+    if variant:
+        meta["variant"] = variant
+    os.makedirs(out, exist_ok=True)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), meta=json.dumps(meta), **arrays)
     print("wrote", name, {k: v.shape for k, v in arrays.items() if k.startswith("in_")})
 
 
@@ -100,6 +105,22 @@ def main():
         itmp = np.zeros_like(img)
         save_case(f"vortex20x14_it{it}_visc", it, vp, tmp, img, itmp, dt=0.1, visc=0.05, steps=3,
                   snap_steps=(1, 3))
+
+    # The reference's clamp mode (its commented-out lines of src/fluid.cpp:44-45,101-102 enabled,
+    # oracle/Makefile): kept apart in golden/clamp/, since the drop-in calls are periodic only.
+    for it in (3, 30):
+        if not O.ref_available(it, "_clamp"):
+            sys.exit(f"oracle/_ref/libfluidref_clamp_it{it}.so missing: run make -C oracle first")
+    clamp_dir = os.path.join(OUT, "clamp")
+    vp, tmp, img, itmp = S.initial_state(32, 24, 3, seed=21)
+    save_case("clamp_vortex32x24_it30", 30, vp, tmp, img, itmp, dt=0.1, visc=0.0, steps=3, snap_steps=(1, 3),
+              variant="_clamp", out=clamp_dir)
+    vp = S.vortex_field(20, 14, 22)
+    vp[..., 2:4] = noisy_scratch((14, 20, 2), 22)
+    tmp = noisy_scratch((14, 20, 4), 122)
+    img = S.blob_image(30, 21, 4, 22)
+    save_case("clamp_vortex20x14_it3_visc", 3, vp, tmp, img, np.zeros_like(img), dt=0.1, visc=0.05, steps=3,
+              snap_steps=(1, 3), variant="_clamp", out=clamp_dir)
 
     # 256x256, 40 sweeps, dt=0.1, 100 steps, 3-channel image, seed 0: digests only.
     vp, tmp, img, itmp = S.initial_state(256, 256, 3, seed=0)

@@ -13,6 +13,11 @@ def cases():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
 
 
+def clamp_cases():
+    """Cases of the reference's clamp mode (golden/clamp)."""
+    return sorted("clamp/" + os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "clamp", "*.npz")))
+
+
 def load(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     meta = json.loads(str(z["meta"]))

@@ -141,3 +141,71 @@ def test_oracle_threads_do_not_change_results(oracle_mod):
     oracle_mod.set_threads(max(old, 1))
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert a[2].rel_residual == b[2].rel_residual
+
+
+# ---- boundary modes -------------------------------------------------------------------------
+
+from golden_util import clamp_cases  # noqa: E402
+
+
+def _run_oracle(oracle_mod, meta, arr, boundary):
+    vp, tmp = arr["in_vp"].copy(), arr["in_tmp"].copy()
+    img, itmp = arr["in_img"].copy(), arr["in_itmp"].copy()
+    out = {}
+    for s in range(1, meta["steps"] + 1):
+        vp, tmp, _ = oracle_mod.step(vp, tmp, meta["dt"], meta["viscosity"], diffuse_iters=meta["iters"],
+                                     max_iters=meta["iters"], boundary=boundary)
+        img, itmp = oracle_mod.advect_color_step(img, itmp, vp, meta["dt"], boundary=boundary)
+        out[s] = (vp.copy(), tmp.copy(), img.copy(), itmp.copy())
+    return out
+
+
+@pytest.mark.parametrize("name", clamp_cases())
+def test_oracle_clamp_matches_reference_clamp_golden(oracle_mod, name):
+    """The restated clamp mode against the reference's own commented clamp
+    lines, enabled (golden/clamp, made from that build)."""
+    meta, arr = load(name)
+    assert meta["variant"] == "_clamp"
+    got = _run_oracle(oracle_mod, meta, arr, boundary=1)
+    for s in meta["snaps"]:
+        for k, a in zip(("vp", "tmp", "img", "itmp"), got[s]):
+            assert np.array_equal(a, arr[f"{k}_s{s}"]), (name, s, k)
+
+
+def test_clamp_cases_exist_and_differ_from_periodic(oracle_mod):
+    assert len(clamp_cases()) >= 2
+    meta, arr = load(clamp_cases()[0])
+    clamp = _run_oracle(oracle_mod, meta, arr, boundary=1)[meta["steps"]]
+    per = _run_oracle(oracle_mod, meta, arr, boundary=0)[meta["steps"]]
+    assert not np.array_equal(clamp[0], per[0])
+
+
+@pytest.mark.parametrize("iters,visc", [(3, 0.05), (30, 0.0)])
+def test_oracle_clamp_matches_reference_clamp_build(oracle_mod, iters, visc):
+    if not oracle_mod.ref_available(iters, "_clamp"):
+        pytest.skip("reference clamp build oracle/_ref not present on this host")
+    vp, tmp, img, itmp = S.initial_state(40, 28, 3, seed=iters)
+    vp[..., 0:2] *= 500.0  # backtraces that leave the grid by several cells
+    a = [vp.copy(), tmp.copy(), img.copy(), itmp.copy()]
+    b = [vp.copy(), tmp.copy(), img.copy(), itmp.copy()]
+    for _ in range(3):
+        a[0], a[1] = oracle_mod.ref_step(iters, a[0], a[1], 0.1, visc, "_clamp")
+        a[2], a[3] = oracle_mod.ref_advect_color_step(iters, a[2], a[3], a[0], 0.1, "_clamp")
+        b[0], b[1], _ = oracle_mod.step(b[0], b[1], 0.1, visc, diffuse_iters=iters, max_iters=iters, boundary=1)
+        b[2], b[3] = oracle_mod.advect_color_step(b[2], b[3], b[0], 0.1, boundary=1)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_oracle_walls_hold_zero_velocity_on_the_boundary(oracle_mod):
+    vp, tmp, img, itmp = S.initial_state(36, 30, 3, seed=4)
+    for _ in range(3):
+        vp, tmp, _ = oracle_mod.step(vp, tmp, 0.1, 0.0, diffuse_iters=2, max_iters=40, boundary=2)
+        img, itmp = oracle_mod.advect_color_step(img, itmp, vp, 0.1, boundary=2)
+        for ch in (0, 1):
+            u = vp[..., ch]
+            assert not u[0].any() and not u[-1].any() and not u[:, 0].any() and not u[:, -1].any()
+            assert u[1:-1, 1:-1].any()
+    with pytest.raises(RuntimeError):
+        oracle_mod.step(np.zeros((1, 5, 4), np.float32), np.zeros((1, 5, 4), np.float32), 0.1, 0.0,
+                        diffuse_iters=1, max_iters=1, boundary=1)  # clamp needs sides >= 2
