@@ -94,6 +94,18 @@ struct Field {
     float *pback = nullptr;             // plain start kept aside while a predicted start is tried
     float *pnet = nullptr;              // the network's correction in the later passes of a predicted start
     Reduce red{};
+    // residual checks run here, overlapping the sweep launch that follows them
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_check = nullptr, ev_res = nullptr;
+
+    int make_aux()
+    {
+        if (aux) return PFS_OK;
+        CK(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ev_check, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_res, cudaEventDisableTiming));
+        return PFS_OK;
+    }
 
     int alloc(int w_, int h_)
     {
@@ -140,6 +152,11 @@ struct Field {
         pback = nullptr;
         if (pnet) cudaFree(pnet);
         pnet = nullptr;
+        if (ev_check) cudaEventDestroy(ev_check);
+        if (ev_res) cudaEventDestroy(ev_res);
+        if (aux) cudaStreamDestroy(aux);
+        aux = nullptr;
+        ev_check = ev_res = nullptr;
         mem = nullptr;
         rmem = nullptr;
         hres = nullptr;
@@ -208,6 +225,14 @@ struct CheckPoint {
 // solve into an immediate return. The host enqueues check intervals in
 // batches that double in size (1, 2, 4, ...) and reads the state only between
 // batches, then takes the plane roles recorded at the converged check point.
+//
+// The residual launch runs on the field's second stream and overlaps the
+// sweep launch that follows it: that launch reads q_S and b, as the residual
+// does, and writes only the third plane. The launch after it (which
+// overwrites q_S or q_{S-1}), any launch writing the q_{S-1} plane, the
+// host's reads of the state and the end of the solve wait for the residual.
+// If the check turns out converged, the one launch that ran meanwhile has
+// written only the plane no role refers to.
 int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStream_t st, int &cur, int &prev)
 {
     cur = f.pidx[X];
@@ -218,6 +243,14 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     const bool resid = c.tol > 0.0;
     const int *done = resid ? &f.dstate->done : nullptr;
     if (resid) CK(cudaMemsetAsync(f.dstate, 0, sizeof(pfs::SolveState), st));
+    if (resid) CKS(f.make_aux());
+    bool pending = false;  // a residual launch on f.aux that st has not waited for
+    int since = 0;         // sweep launches since the last check
+    auto settle = [&]() -> int {
+        if (pending) CK(cudaStreamWaitEvent(st, f.ev_res, 0));
+        pending = false;
+        return PFS_OK;
+    };
 
     CheckPoint marks[64];
     int nmarks = 0, batch = 1, in_batch = 0;
@@ -231,7 +264,9 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
         if (resid && c.check_every > 0) stop = std::min(c.S, (S / c.check_every + 1) * c.check_every);
         while (S < stop) {
             if (!fused) {
+                if (pending && since >= 1) CKS(settle());
                 CK(pfs::launch_sweep_single(f.p[cur], f.b, f.p[freep], f.ld, f.w, f.h, done, st));
+                ++since;
                 const int old_prev = prev;
                 prev = cur;
                 cur = freep;
@@ -241,17 +276,25 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
             }
             const int n = std::min(L, stop - S);
             const bool last = (S + n == stop);
+            if (pending && (since >= 1 || last)) CKS(settle());
             CK(pfs::launch_sweep_stream(f.p[cur], f.b, f.p[freep], last ? f.p[prev] : nullptr, f.ld, f.w, f.h, n,
                                         c.tun.halo, c.tun.chunk, done, st));
+            ++since;
             const int old_cur = cur;
             cur = freep;  // q_S; after a `last` launch prev holds q_{S-1}
             freep = old_cur;
             S += n;
         }
         if (!resid) break;
-        CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, st));
+        CK(cudaEventRecord(f.ev_check, st));
+        CK(cudaStreamWaitEvent(f.aux, f.ev_check, 0));
+        CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, f.aux));
+        CK(cudaEventRecord(f.ev_res, f.aux));
+        pending = true;
+        since = 0;
         marks[nmarks++] = {S, cur, prev};
         if (++in_batch == batch || S == c.S || nmarks == 64 || watch) {
+            CKS(settle());
             CK(cudaMemcpyAsync(f.hstate, f.dstate, sizeof(pfs::SolveState), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             if (f.hstate->done || S == c.S) finished = true;
@@ -270,6 +313,7 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
             batch = std::min(batch * 2, 16);
         }
     }
+    CKS(settle());
     if (resid && nmarks > 0) {
         const pfs::SolveState &hs = *f.hstate;  // copied at the last sync
         o.checks = hs.checks;
