@@ -312,6 +312,12 @@ int pfs_ensemble_config(pfs_ensemble *e, int fuse_depth, int chunk_rows);
 int pfs_ensemble_info(pfs_ensemble *e, int *fuse_depth, int *chunk_rows, int *grid_blocks, int *graphs);
 /* restore == 0: copy the whole state aside (device to device); 1: put it back */
 int pfs_ensemble_snapshot(pfs_ensemble *e, int restore);
+/* Test hook for the bounded grid barrier: in the next pfs_ensemble_step,
+ * block `block` of the step kernel leaves at once without reaching the first
+ * barrier, so the other blocks' bounded wait runs out (about 1-2 s), they
+ * return, and the step returns PFS_ERR_DEVICE_TIMEOUT (no fault, no hang).
+ * The ensemble then stays failed: every later step returns the same status. */
+int pfs_ensemble_debug_stall_block(pfs_ensemble *e, int block);
 /* Ensemble statistics of the image field: for every pixel and channel, the
  * mean and the population variance (divide by n) over the n listed members,
  * which must share one grid size; FP64 accumulation in list order, float32

@@ -71,6 +71,7 @@ struct EnsArgs {
     float dt, gamma;
     double tol;
     int cap, check_every, chunk, channels, icur;
+    int stall_block;  // test hook: this block leaves at once (-1: none); see pfs_ensemble_debug_stall_block
 };
 
 constexpr int kRowsPerTask = 8;
@@ -130,6 +131,8 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * 4 + wib, nw = gridDim.x * 4;
     V *ring = reinterpret_cast<V *>(sm_raw) + wib * Ring<float, L>::vecs_per_warp;
+    // test hook: a block that never reaches the first barrier, so the others' bounded wait runs out
+    if ((int)blockIdx.x == a.stall_block) return;
     const int ic = a.icur, io = 1 - a.icur;
 
     // advect every member: u[0], v[0] -> u[1], v[1]
@@ -276,6 +279,7 @@ struct Ensemble {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool graphs_ok = true;
     int *dsel = nullptr;  // member list of pfs_ensemble_image_stats (n ints)
+    int stall_block = -1;  // test hook for the next step (pfs_ensemble_debug_stall_block)
 };
 
 namespace {
@@ -398,6 +402,7 @@ EnsArgs make_args(Ensemble &E, int icur)
     a.check_every = E.prm.check_every > 0 ? E.prm.check_every : E.prm.max_iters;
     a.chunk = E.chunk;
     a.channels = E.c;
+    a.stall_block = E.stall_block;
     a.icur = icur;
     return a;
 }
@@ -427,6 +432,12 @@ int build_graphs(Ensemble &E)
 {
     drop_graphs(E);
     if (!E.graphs_ok) return PFS_OK;
+    struct NoStall {  // the captured steps never carry the test hook
+        Ensemble &e;
+        int saved;
+        explicit NoStall(Ensemble &x) : e(x), saved(x.stall_block) { e.stall_block = -1; }
+        ~NoStall() { e.stall_block = saved; }
+    } no_stall(E);
     cudaStream_t cs;
     ECK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     for (int par = 0; par < 2; ++par) {
@@ -703,7 +714,12 @@ int pfs_ensemble_step(pfs_ensemble *e, int steps)
     }
     for (int s = 0; s < steps; ++s) {
         cudaError_t r;
-        if (E->graphs_ok && E->graph[E->icur]) {
+        if (E->stall_block >= 0) {  // test hook: a direct launch with the stalling block, once
+            int rc = pfs::enqueue_step(*E, E->icur, E->st);
+            E->stall_block = -1;
+            if (rc != PFS_OK) return rc;
+            r = cudaSuccess;
+        } else if (E->graphs_ok && E->graph[E->icur]) {
             r = cudaGraphLaunch(E->graph[E->icur], E->st);
             if (r == cudaSuccess) pfs::launched();
         } else {
@@ -720,6 +736,14 @@ int pfs_ensemble_step(pfs_ensemble *e, int steps)
     if (r == cudaSuccess) r = cudaStreamSynchronize(E->st);
     if (r != cudaSuccess) return pfs::record_error(PFS_ERR_CUDA, cudaGetErrorString(r));
     if (err) return pfs::record_error(PFS_ERR_DEVICE_TIMEOUT, "ensemble grid barrier timed out");
+    return PFS_OK;
+}
+
+int pfs_ensemble_debug_stall_block(pfs_ensemble *e, int block)
+{
+    Ensemble *E = reinterpret_cast<Ensemble *>(e);
+    if (!E || block < 0) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad arguments");
+    E->stall_block = block;
     return PFS_OK;
 }
 

@@ -20,6 +20,7 @@ raises.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 from dataclasses import dataclass
 from typing import Optional, Tuple
@@ -120,6 +121,7 @@ SIGNATURES = [
     ("pfs_ensemble_info", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                     C.POINTER(C.c_int)]),
     ("pfs_ensemble_snapshot", C.c_int, [C.c_void_p, C.c_int]),
+    ("pfs_ensemble_debug_stall_block", C.c_int, [C.c_void_p, C.c_int]),
     ("pfs_ensemble_image_stats", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p,
                                            C.c_int]),
     ("pfs_ensemble_destroy", C.c_int, [C.c_void_p]),
@@ -292,6 +294,33 @@ class Session:
         _check(lib().pfs_session_stats(self._h, C.byref(s)))
         return s.as_dict()
 
+    def checkpoint(self, path: str):
+        """Write the state (both velocity buffers with channels 2-3, the image)
+        and the parameters to an .npz file. For the float32 form this is the
+        whole state: restoring it into a session with the same parameters and
+        stepping on gives the same bits as never stopping. The refined forms
+        keep their pressure in FP64, which this float32 snapshot rounds."""
+        h, w = self.h, self.w
+        vp, tmp = np.empty((h, w, 4), np.float32), np.empty((h, w, 4), np.float32)
+        ih, iw, ic = self.image_shape
+        img = np.empty((ih, iw, ic), np.float32) if ic else None
+        self.download(vp, tmp, img)
+        st = self.stats()
+        params = {k: getattr(self.params, k) for k, _ in Params._fields_}
+        np.savez(path, vp=vp, tmp=tmp, image=img if img is not None else np.zeros(0, np.float32),
+                 params=json.dumps(params), steps=st["steps"])
+
+    @classmethod
+    def restore(cls, path: str, stream: int = 0) -> "Session":
+        """A new session holding a checkpoint's state and parameters."""
+        z = np.load(path)
+        vp, tmp, img = z["vp"], z["tmp"], z["image"]
+        params = default_params(**json.loads(str(z["params"])))
+        h, w, _ = vp.shape
+        s = cls(w, h, image_shape=img.shape if img.size else None, params=params, stream=stream)
+        s.upload(vp, tmp, img if img.size else None)
+        return s
+
     def set_start(self, mode: int, net: "UNet" = None, coarsen: int = 1, passes: int = 1):
         """Initial pressure of each step: START_PREVIOUS (reference), START_ZERO,
         START_NETWORK (the network run on the grid coarsened `coarsen` times,
@@ -411,6 +440,10 @@ class Ensemble:
         _check(lib().pfs_ensemble_download(self._h, k, C.c_void_p(_ptr(vp) if vp is not None else None),
                                            C.c_void_p(_ptr(image) if image is not None else None), where))
         return vp, image
+
+    def debug_stall_block(self, block: int):
+        """Test hook: block `block` skips the next step's grid barriers (the step then times out)."""
+        _check(lib().pfs_ensemble_debug_stall_block(self._h, int(block)))
 
     def image_stats(self, members, mean=None, var=None):
         """Pointwise mean and population variance of the image over `members`

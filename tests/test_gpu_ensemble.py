@@ -122,3 +122,35 @@ def test_ensemble_image_statistics_match_sessions(cuda_device, pfs_lib):
     assert np.abs(var - ref_var).max() <= 1e-6 * max(ref_var.max(), 1e-12) + 1e-9
     assert np.array_equal(sub_mean, imgs[0].astype(np.float32))
     assert var.max() > 0.0
+
+
+def test_grid_barrier_timeout_is_reported(cuda_device, pfs_lib):
+    """Failure detection without a GPU fault: one block of the step kernel
+    leaves before the first grid barrier, the others' bounded wait runs out
+    (~1-2 s), every block returns, and the step reports PFS_ERR_DEVICE_TIMEOUT.
+    The failed ensemble stays failed; the device stays usable."""
+    import time
+    sizes = [(64, 64), (96, 40)]
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=64, tol=1e-3, check_every=32)
+    states = [member_state(w, h, k) for k, (w, h) in enumerate(sizes)]
+    with pfs_lib.Ensemble(sizes, 3, **kw) as ens:
+        for k, st in enumerate(states):
+            ens.upload(k, *st)
+        ens.step(1)  # a normal step first (graphs built)
+        ens.debug_stall_block(0)
+        t0 = time.time()
+        with pytest.raises(pfs_lib.PFSError) as ei:
+            ens.step(1)
+        assert ei.value.status == 6  # PFS_ERR_DEVICE_TIMEOUT
+        assert time.time() - t0 < 60
+        with pytest.raises(pfs_lib.PFSError):
+            ens.step(1)  # sticky
+    # the device is fine: a new ensemble steps and matches a session
+    with pfs_lib.Ensemble(sizes, 3, **kw) as ens:
+        for k, st in enumerate(states):
+            ens.upload(k, *st)
+        ens.step(2)
+        a, c = np.empty_like(states[1][0]), np.empty_like(states[1][2])
+        ens.download(1, a, c)
+    ref = session_run(pfs_lib, *states[1], 2, **kw)
+    assert np.array_equal(a[..., :2], ref[0][..., :2]) and np.array_equal(c, ref[2])

@@ -235,3 +235,28 @@ def test_trained_network_saves_sweeps_at_256(cuda_device, pfs_lib):
     print(r["zero"]["mean_sweeps"], n["mean_sweeps"], n["sweeps_saved"], n["time_ratio"])
     assert n["fallbacks"] == 0
     assert n["sweeps_saved"] > 0.08
+
+
+@pytest.mark.parametrize("tol", [0.0, 1e-4])
+def test_checkpoint_resume_is_bit_exact(cuda_device, pfs_lib, tmp_path, tol):
+    """5 steps straight through equal 2 steps, checkpoint, restore into a new
+    session, 3 steps (float32 form: the snapshot is the whole state)."""
+    vp, tmp, img, _ = S.initial_state(96, 64, 3, seed=8)
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=300 if tol else 31, tol=tol, check_every=50 if tol else 0)
+    with pfs_lib.Session(96, 64, image_shape=img.shape, **kw) as s:
+        s.upload(vp, tmp, img)
+        s.step(5)
+        want = [np.empty_like(vp), np.empty_like(tmp), np.empty_like(img)]
+        s.download(*want)
+    path = str(tmp_path / "ck.npz")
+    with pfs_lib.Session(96, 64, image_shape=img.shape, **kw) as s:
+        s.upload(vp, tmp, img)
+        s.step(2)
+        s.checkpoint(path)
+    with pfs_lib.Session.restore(path) as s:
+        assert s.params.max_iters == kw["max_iters"] and s.params.tol == tol
+        s.step(3)
+        got = [np.empty_like(vp), np.empty_like(tmp), np.empty_like(img)]
+        s.download(*got)
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
