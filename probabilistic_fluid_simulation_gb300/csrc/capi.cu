@@ -867,11 +867,8 @@ int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const 
     f.pidx[1] = 1;
     s->vpSlot = 0;
     s->tmpSlot = 1;
-    CK(pfs::launch_split_velocity(A, f.u[0], f.v[0], f.ld, f.w, f.h, s->st));
-    CK(pfs::launch_split_velocity(B, f.u[1], f.v[1], f.ld, f.w, f.h, s->st));
-    CK(pfs::launch_split_channel(A, 2, 4, f.p[0], f.ld, f.w, f.h, s->st));
-    CK(pfs::launch_split_channel(B, 2, 4, f.p[1], f.ld, f.w, f.h, s->st));
-    CK(pfs::launch_split_channel(A, 3, 4, f.b, f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_vp(A, f.u[0], f.v[0], f.p[0], f.b, f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_vp(B, f.u[1], f.v[1], f.p[1], nullptr, f.ld, f.w, f.h, s->st));
     if (s->ic > 0) {
         s->icur = 0;
         CK(pfs::launch_split_image(I, s->img[0], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));

@@ -70,6 +70,9 @@ cudaError_t launch_advect_image_interleaved(const float *img, float *imgo, int i
                                             const float *vel, int vw, int vh, float dt, cudaStream_t st);
 // interleaved (h, w, 4) <-> planar
 cudaError_t launch_split_velocity(const float *vp, float *u, float *v, int ld, int w, int h, cudaStream_t st);
+// interleaved (u, v, p, b) -> planes in one pass (b may be null)
+cudaError_t launch_split_vp(const float *vp, float *u, float *v, float *p, float *b, int ld, int w, int h,
+                            cudaStream_t st);
 cudaError_t launch_split_channel(const float *buf, int ch, int nch, float *plane, int ld, int w, int h,
                                  cudaStream_t st);
 cudaError_t launch_merge_velocity(float *out, const float *u, const float *v, const float *p, const float *b,

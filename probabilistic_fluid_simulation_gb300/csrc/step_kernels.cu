@@ -195,6 +195,22 @@ __global__ void k_split_channel(const float *__restrict__ buf, int ch, int nch, 
     plane[(size_t)j * ld + i] = buf[((size_t)j * w + i) * nch + ch];
 }
 
+// One interleaved (u, v, p, b) buffer into its planes, each cell read once
+// (b may be null). The source may be host memory mapped into the device's
+// address space: each 16-byte cell crosses the link once.
+__global__ void k_split_vp(const float4 *__restrict__ vp, float *__restrict__ u, float *__restrict__ v,
+                           float *__restrict__ p, float *__restrict__ b, int ld, int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const float4 q = vp[(size_t)j * w + i];
+    const size_t o = (size_t)j * ld + i;
+    u[o] = q.x;
+    v[o] = q.y;
+    p[o] = q.z;
+    if (b) b[o] = q.w;
+}
+
 __global__ void k_merge_velocity(float4 *__restrict__ out, const float *__restrict__ u, const float *__restrict__ v,
                                  const float *__restrict__ p, const float *__restrict__ b, int ld, int w, int h)
 {
@@ -403,6 +419,13 @@ cudaError_t launch_advect_image_interleaved(const float *img, float *imgo, int i
 cudaError_t launch_split_velocity(const float *vp, float *u, float *v, int ld, int w, int h, cudaStream_t st)
 {
     k_split_velocity<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(reinterpret_cast<const float4 *>(vp), u, v, ld, w, h);
+    return launched();
+}
+
+cudaError_t launch_split_vp(const float *vp, float *u, float *v, float *p, float *b, int ld, int w, int h,
+                            cudaStream_t st)
+{
+    k_split_vp<<<grid2d(w, h), dim3(kBX, kBY), 0, st>>>(reinterpret_cast<const float4 *>(vp), u, v, p, b, ld, w, h);
     return launched();
 }
 
