@@ -396,12 +396,14 @@ def warm_start_form(a, fluid, stream):
     Wall time per step includes the network's inference and damped passes."""
     from probabilistic_fluid_simulation_gb300 import warmstart as WS
     params, meta = WS.load_default()
-    out = {"workload": "states of 8-vortex fields (seeds 0, 1; steps 1, 2; dt 0.1) at 256x256 and 1024x1024, "
-                       "one step each from zero pressure to relative residual 1e-5, PFS_PREC_F32R",
+    out = {"workload": "states of 8-vortex fields (seeds 0, 1; steps 1, 2 at 256x256 and 1024x1024, step 1 at "
+                       "2048x2048; dt 0.1), one step each from zero pressure to relative residual 1e-5, "
+                       "PFS_PREC_F32R",
            "network": {"trained_on": f"{meta['pairs']} solver pairs at {meta['size']}x{meta['size']}",
                        "held_out_loss": meta["training"]["val_loss"][-1]}}
-    for size, (coarsen, passes), every in ((256, (1, 2), 200), (1024, (4, 1), 500)):
-        r = WS.evaluate(params, size, [0, 1], steps=2, check_every=every, starts=((coarsen, passes),),
+    for size, (coarsen, passes), every, steps in ((256, (1, 2), 200, 2), (1024, (4, 1), 500, 2),
+                                                 (2048, (8, 1), 1000, 1)):
+        r = WS.evaluate(params, size, [0, 1], steps=steps, check_every=every, starts=((coarsen, passes),),
                         log=lambda *_: None)
         z, n = r["zero"], r["network"][f"coarsen{coarsen}_passes{passes}"]
         out[str(size)] = {

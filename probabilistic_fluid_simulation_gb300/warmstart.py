@@ -196,6 +196,8 @@ def eval_states(size, seeds, steps, dt=0.1, tol=1e-5, cap=2_000_000, check_every
             s.upload(vp, zeros)
             for k in range(steps):
                 states.append(vp.copy())
+                if steps == 1:
+                    break  # one state per seed: nothing to step for
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
                 s.step(1)
