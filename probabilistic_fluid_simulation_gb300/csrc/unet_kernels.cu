@@ -119,57 +119,108 @@ __global__ void __launch_bounds__(128) k_conv3x3(Tensor in, const bf16 *__restri
     }
 }
 
-// Weight gradient of a 3x3 conv: dW[co][tap][ci] += sum_pixels dY[p][co] * X[p + tap][ci],
-// dB[co] += sum dY[p][co]. A block owns a 16 (co) x 16 (ci) x 9 (tap) slice and
-// a range of image rows; rows are staged in shared memory (three input rows
-// and one dY row per output row), each thread accumulates its (co, ci) pair's
-// nine taps in registers, then adds them to the fp32 gradient.
-constexpr int kWgRows = 8;  // output rows per block
-__global__ void __launch_bounds__(256) k_wgrad3x3(Tensor x, const bf16 *__restrict__ dy, int cout, int cin, int cinp,
-                                                 float *__restrict__ dw, float *__restrict__ db, int n_img, int H,
-                                                 int W)
+// Weight gradient of a 3x3 conv on the tensor cores. Per tap t,
+// dW_t[co][ci] += sum_p dY[p][co] X[shift_t(p)][ci]: a GEMM with M = cout,
+// N = cin and K = pixels. A block owns a 32 (co) x 32 (ci) tile for all nine
+// taps and a run of row segments of up to 128 pixels; per segment dY
+// (pixels x 32 co) and the three input rows the taps read (pixels + 2 x 32
+// ci, circular halo) are staged in shared memory as [pixel][channel] tiles,
+// from which ldmatrix.trans yields both operands (the pixel dimension is
+// strided in memory for both). Four warps, each a 16 x 16 (co, ci) quarter
+// of the tile, 9 taps x 2 n-tiles of fp32 accumulators; the block adds its
+// partial sums to dW with atomics. Rows of 40 bf16 (80 bytes) keep the
+// ldmatrix row reads free of bank conflicts.
+constexpr int kWgSeg = 128;  // pixels per row segment (at most)
+constexpr int kWgLd = 40;    // shared-memory row pitch, bf16
+
+__device__ __forceinline__ void ldsm_x4_trans(unsigned (&r)[4], const bf16 *p)
 {
-    extern __shared__ float smem[];
-    float *sx = smem;                 // [3][W][16]
-    float *sd = smem + 3 * W * 16;    // [W][16]
-    const int co0 = blockIdx.y * 16, ci0 = blockIdx.z * 16;
-    const int tco = threadIdx.x >> 4, tci = threadIdx.x & 15;
-    const int total_rows = n_img * H;
-    float acc[9];
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+// Eight channels of one pixel (channels c..c+7 below `lim` are real, the rest zero).
+__device__ __forceinline__ uint4 load8(const bf16 *p, int c, int lim, bool vec)
+{
+    if (vec && c + 8 <= lim) return *reinterpret_cast<const uint4 *>(p + c);
+    __align__(16) bf16 v[8];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) acc[k] = 0.f;
-    float accb = 0.f;
-    for (int row = blockIdx.x * kWgRows; row < min(total_rows, (blockIdx.x + 1) * kWgRows); ++row) {
-        const int img = row / H, y = row % H;
-        __syncthreads();
-        for (int e = threadIdx.x; e < 3 * W * 16; e += blockDim.x) {
-            const int r = e / (W * 16), xx = (e / 16) % W, c = e % 16;
-            const int yy = wrapi(y + r - 1, H);
-            const int ci = ci0 + c;
-            sx[e] = ci < cin ? __bfloat162float(x.p[(((size_t)img * H + yy) * W + xx) * x.stride + x.off + ci]) : 0.f;
-        }
-        for (int e = threadIdx.x; e < W * 16; e += blockDim.x) {
-            const int xx = e / 16, c = e % 16;
-            const int co = co0 + c;
-            sd[e] = co < cout ? __bfloat162float(dy[(((size_t)img * H + y) * W + xx) * cout + co]) : 0.f;
-        }
-        __syncthreads();
-        for (int xx = 0; xx < W; ++xx) {
-            const float g = sd[xx * 16 + tco];
-            accb += g;
+    for (int k = 0; k < 8; ++k) v[k] = (c + k < lim) ? p[c + k] : __float2bfloat16_rn(0.f);
+    return *reinterpret_cast<const uint4 *>(v);
+}
+
+__global__ void __launch_bounds__(128) k_wgrad_tc(Tensor x, const bf16 *__restrict__ dy, int cout, int cin, int cinp,
+                                                 float *__restrict__ dw, float *__restrict__ db, int n_img, int H,
+                                                 int W, int seg_len, int segs_per_block)
+{
+    __shared__ __align__(16) bf16 sD[kWgSeg][kWgLd];
+    __shared__ __align__(16) bf16 sX[3][kWgSeg + 2][kWgLd];
+    const int co0 = blockIdx.y * 32, ci0 = blockIdx.z * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wm = (warp & 1) * 16, wn = (warp >> 1) * 16;  // warp's co / ci offsets in the tile
+    const bool xvec = (x.stride % 8 == 0) && (x.off % 8 == 0);
+    const int segs_per_row = W / seg_len, total = n_img * H * segs_per_row;
+    float acc[9][2][4];
 #pragma unroll
-            for (int tap = 0; tap < 9; ++tap) {
-                const int xs = wrapi(xx + tap % 3 - 1, W);
-                acc[tap] = fmaf(g, sx[((tap / 3) * W + xs) * 16 + tci], acc[tap]);
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int n = 0; n < 2; ++n) acc[t][n][0] = acc[t][n][1] = acc[t][n][2] = acc[t][n][3] = 0.f;
+
+    // bias gradient (blocks of the first ci tile): column sums of the staged dY tiles, thread t takes
+    // channel co0 + t % 32 and every fourth pixel from t / 32
+    const bool bias = db && blockIdx.z == 0;
+    float bsum = 0.f;
+    const int s_beg = blockIdx.x * segs_per_block, s_end = min(total, s_beg + segs_per_block);
+    for (int sg = s_beg; sg < s_end; ++sg) {
+        const int img = sg / (H * segs_per_row), rem = sg - img * H * segs_per_row;
+        const int y = rem / segs_per_row, x0 = (rem % segs_per_row) * seg_len;
+        __syncthreads();  // the previous segment's tiles are consumed
+        for (int e = threadIdx.x; e < seg_len * 4; e += blockDim.x) {  // dY: seg_len px x 4 chunks of 8 co
+            const int px = e >> 2, part = e & 3;
+            const bf16 *src = dy + (((size_t)img * H + y) * W + x0 + px) * cout;
+            *reinterpret_cast<uint4 *>(&sD[px][part * 8]) = load8(src, co0 + part * 8, cout, true);
+        }
+        for (int e = threadIdx.x; e < 3 * (seg_len + 2) * 4; e += blockDim.x) {  // X: 3 rows x (seg_len + 2) px
+            const int r = e / ((seg_len + 2) * 4), q = e - r * (seg_len + 2) * 4;
+            const int px = q >> 2, part = q & 3;
+            const int yy = wrapi(y + r - 1, H), xx = wrapi(x0 + px - 1, W);
+            const bf16 *src = x.p + (((size_t)img * H + yy) * W + xx) * x.stride + x.off;
+            *reinterpret_cast<uint4 *>(&sX[r][px][part * 8]) = load8(src, ci0 + part * 8, cin, xvec);
+        }
+        __syncthreads();
+        if (bias)
+            for (int px = threadIdx.x >> 5; px < seg_len; px += 4) bsum += __bfloat162float(sD[px][threadIdx.x & 31]);
+        for (int k0 = 0; k0 < seg_len; k0 += 16) {
+            unsigned a[4];
+            ldsm_x4_trans(a, &sD[k0 + (lane >> 4) * 8 + (lane & 7)][wm + ((lane >> 3) & 1) * 8]);
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+                unsigned b[4];
+                ldsm_x4_trans(b, &sX[t / 3][k0 + t % 3 + ((lane >> 3) & 1) * 8 + (lane & 7)][wn + (lane >> 4) * 8]);
+                const unsigned b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+                mma16816(acc[t][0], a, b0);
+                mma16816(acc[t][1], a, b1);
             }
         }
     }
-    const int co = co0 + tco, ci = ci0 + tci;
-    if (co < cout && ci < cin) {
+    // accumulator (m16n8): [0..1] -> co = lane / 4, ci = 2 (lane % 4) + {0, 1}; [2..3] -> co + 8
+    const int cr = lane >> 2, cc = (lane & 3) * 2;
 #pragma unroll
-        for (int tap = 0; tap < 9; ++tap) atomicAdd(dw + ((size_t)co * 9 + tap) * cinp + ci, acc[tap]);
-    }
-    if (db && ci0 == 0 && tci == 0 && co < cout) atomicAdd(db + co, accb);
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int n = 0; n < 2; ++n)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int co = co0 + wm + cr + h * 8;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const int ci = ci0 + wn + n * 8 + cc + j;
+                    if (co < cout && ci < cin) atomicAdd(dw + ((size_t)co * 9 + t) * cinp + ci, acc[t][n][h * 2 + j]);
+                }
+            }
+    if (bias && co0 + (threadIdx.x & 31) < cout) atomicAdd(db + co0 + (threadIdx.x & 31), bsum);
 }
 
 // 2x2 average pooling (bf16 -> bf16) and its backward (fp32, added).
@@ -451,16 +502,16 @@ cudaError_t conv3x3(Tensor in, int cin, const bf16 *w, const float *bias, Tensor
 cudaError_t wgrad3x3(Tensor x, int cin, int cinp, const bf16 *dy, int cout, float *dw, float *db, int n, int H, int W,
                      cudaStream_t st)
 {
-    const size_t smem = sizeof(float) * 4 * W * 16;
-    static int max_set = 0;
-    if ((int)smem > max_set) {
-        const cudaError_t e = cudaFuncSetAttribute(k_wgrad3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (e != cudaSuccess) return e;
-        max_set = 200 * 1024;
-    }
-    if (smem > 200 * 1024) return cudaErrorInvalidValue;
-    dim3 grid((n * H + kWgRows - 1) / kWgRows, (cout + 15) / 16, (cin + 15) / 16);
-    k_wgrad3x3<<<grid, 256, smem, st>>>(x, dy, cout, cin, cinp, dw, db, n, H, W);
+    if (W % 16 || cout % 8) return cudaErrorInvalidValue;
+    const int seg_len = W < kWgSeg ? W : kWgSeg;
+    if (W % seg_len) return cudaErrorInvalidValue;
+    const int total = n * H * (W / seg_len);
+    // about one block per SM per (co, ci) tile: each block's atomics are amortised over many segments
+    const int tiles = ((cout + 31) / 32) * ((cin + 31) / 32);
+    const int want = (2 * 152 + tiles - 1) / tiles;
+    const int per = (total + want - 1) / want;
+    dim3 grid((total + per - 1) / per, (cout + 31) / 32, (cin + 31) / 32);
+    k_wgrad_tc<<<grid, 128, 0, st>>>(x, dy, cout, cin, cinp, dw, db, n, H, W, seg_len, per);
     return launched();
 }
 

@@ -3,6 +3,7 @@
     python -m probabilistic_fluid_simulation_gb300.warmstart train --pairs 20000 --epochs 4 --out weights.npz
     python -m probabilistic_fluid_simulation_gb300.warmstart eval --weights weights.npz --size 1024 --starts 4x1
     python -m probabilistic_fluid_simulation_gb300.warmstart export --out unet.bin
+    python -m probabilistic_fluid_simulation_gb300.warmstart bench-net --size 256 --batch 16
 
 Training pairs come from the solver itself: members of the 256x256 workload
 (8 seeded Gaussian vortices, dt 0.1) are stepped by the ensemble solver with
@@ -269,6 +270,57 @@ def evaluate(params, size, seeds, steps=3, dt=0.1, tol=1e-5, cap=4_000_000, chec
     return out
 
 
+# Multiply-adds x 2 per pixel of the network's forward pass, from the layer table
+# (3x3 convolutions with the input channels padded to 16, the 1x1 head).
+_LAYERS = [(1, 16, 0), (16, 16, 0), (16, 32, 1), (32, 32, 1), (32, 64, 2), (64, 64, 2), (64, 64, 3), (64, 64, 3),
+           (128, 64, 2), (64, 64, 2), (96, 32, 1), (32, 32, 1), (48, 16, 0), (16, 16, 0)]
+FORWARD_FLOP_PER_PIXEL = sum(2 * 9 * max(ci, 16) * co / 4 ** lv for ci, co, lv in _LAYERS) + 2 * 16
+
+
+def bench_network(size=256, batch=16, reps=20, log=print):
+    """Time a training step (forward + backward + Adam) on `batch` random
+    smooth pairs at size x size and a prediction at size x size; report
+    algorithmic TFLOP/s (forward FORWARD_FLOP_PER_PIXEL per pixel, backward
+    twice that)."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(0)
+    b = torch.randn(batch, size, size, generator=g).cuda()
+    p = torch.randn(batch, size, size, generator=g).cuda()
+    net = fluid.UNet(batch * size * size)
+    net.set_params(init_params(net.n_params))
+    out = torch.empty(size, size, device="cuda")
+    train = True
+    for _ in range(3):
+        if train:
+            net.forward_backward(b, p)
+            net.adam_step(1e-4)
+        net.predict(b[0], out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    train_ms = None
+    if train:
+        e0.record()
+        for _ in range(reps):
+            net.forward_backward(b, p)
+            net.adam_step(1e-4)
+        e1.record()
+        torch.cuda.synchronize()
+        train_ms = e0.elapsed_time(e1) / reps
+    e0.record()
+    for _ in range(reps):
+        net.predict(b[0], out)
+    e1.record()
+    torch.cuda.synchronize()
+    pred_ms = e0.elapsed_time(e1) / reps
+    px = batch * size * size
+    r = {"size": size, "batch": batch, "forward_flop_per_pixel": FORWARD_FLOP_PER_PIXEL,
+         "train_step_ms": train_ms,
+         "train_tflops": 3 * FORWARD_FLOP_PER_PIXEL * px / (train_ms / 1e3) / 1e12 if train_ms else None,
+         "predict_ms": pred_ms, "predict_tflops": FORWARD_FLOP_PER_PIXEL * size * size / (pred_ms / 1e3) / 1e12}
+    log(json.dumps(r))
+    return r
+
+
 def summary(r):
     return {"size": r["size"], "zero_sweeps": r["zero"]["mean_sweeps"],
             **{k: {kk: v[kk] for kk in ("mean_sweeps", "sweeps_saved", "time_ratio", "fallbacks")}
@@ -293,6 +345,10 @@ def main():
     t.add_argument("--eval-steps", type=int, default=3)
     t.add_argument("--eval-sizes", type=int, nargs="*", default=[256])
     t.add_argument("--eval-starts", default="1x1", help="network starts to evaluate: coarsening x passes, ...")
+    nb = sub.add_parser("bench-net", help="time the network's training step and prediction")
+    nb.add_argument("--size", type=int, default=256)
+    nb.add_argument("--batch", type=int, default=16)
+    nb.add_argument("--reps", type=int, default=20)
     x = sub.add_parser("export", help="write the shipped parameters as raw little-endian float32")
     x.add_argument("--weights", default=DEFAULT_WEIGHTS)
     x.add_argument("--out", required=True)
@@ -320,6 +376,8 @@ def main():
             meta[f"eval_{size}"] = r
             save(a.out, params, meta)
             print(json.dumps(summary(r)))
+    elif a.cmd == "bench-net":
+        bench_network(a.size, a.batch, a.reps)
     elif a.cmd == "export":
         params, _ = load(a.weights)
         params.astype("<f4").tofile(a.out)

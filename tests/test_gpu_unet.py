@@ -92,3 +92,16 @@ def test_unet_training_reduces_loss(cuda_device, pfs_lib):
         net.adam_step(1e-3)
     last = net.forward_backward(bt, pt)
     assert last < 0.2 * first, (first, last)
+
+
+def test_unet_trains_on_wide_grids(cuda_device, pfs_lib):
+    """The weight gradient streams row segments of at most 128 pixels, so
+    training takes any width (here 1024) and gives finite gradients."""
+    import torch
+    net = pfs_lib.UNet(128 * 1024)
+    rng = np.random.default_rng(1)
+    net.set_params((rng.standard_normal(net.n_params) * 0.05).astype(np.float32))
+    b, p = smooth_batch(1, 128, 1024, seed=3)
+    loss = net.forward_backward(torch.from_numpy(b).cuda(), torch.from_numpy(p).cuda())
+    g = net.grads()
+    assert np.isfinite(loss) and loss > 0 and np.isfinite(g).all() and np.abs(g).max() > 0
