@@ -79,8 +79,8 @@ def build_cli(force: bool = False) -> str:
             raise RuntimeError(f"g++ failed for the PNG codec:\n{r.stdout}\n{r.stderr}")
     main = os.path.join(CLI_DIR, "fluidsim.cpp")
     if force or _stale(CLI_BIN, deps + [main, LIB, os.path.join(INCLUDE, "pfs.h")]):
-        cmd = [gxx] + flags + [main] + png + ["-I", INCLUDE, "-L", PKG, "-lpfs_gb300", "-Wl,-rpath,$ORIGIN",
-                                              "-o", CLI_BIN]
+        cmd = [gxx] + flags + ["-pthread", main] + png + ["-I", INCLUDE, "-L", PKG, "-lpfs_gb300",
+                                                          "-Wl,-rpath,$ORIGIN", "-o", CLI_BIN]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"g++ failed for the driver:\n{r.stdout}\n{r.stderr}")

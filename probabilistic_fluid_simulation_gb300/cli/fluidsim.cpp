@@ -15,16 +15,23 @@
 // environment variable PFS_JACOBI_ITERS (default 30).
 //
 // Differences from the reference, on purpose: the elapsed time is taken after
-// the device has finished (src/main.cpp:247-254 reads the clock before its
-// cudaDeviceSynchronize); a missing output directory is created; a failing
-// read, write or CUDA call ends the run with a message and exit status 1.
+// the device has finished and every frame is written (src/main.cpp:247-254
+// reads the clock before its cudaDeviceSynchronize); frames are compressed
+// and written by worker threads while the steps go on; a missing output
+// directory is created; a failing read, write or CUDA call ends the run with
+// a message and exit status 1.
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
+#include <deque>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pfs.h"
@@ -60,6 +67,72 @@ uint8_t to_byte(float x)
     if (v >= 255.0) return 255;
     return (uint8_t)v;  // truncation, as the reference's cast
 }
+
+// Encodes and writes the per-step PNGs on worker threads, so the steps go on
+// while earlier frames are compressed (the frames are independent). The queue
+// is bounded; the first failure is kept and reported by finish().
+class PngWriters {
+  public:
+    PngWriters(int width, int height, int threads, size_t max_queued)
+        : w_(width), h_(height), max_queued_(max_queued)
+    {
+        for (int k = 0; k < threads; ++k) pool_.emplace_back([this] { run(); });
+    }
+    ~PngWriters() { finish(); }
+    void submit(std::string path, std::vector<uint8_t> rgba)
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        room_.wait(lk, [this] { return jobs_.size() < max_queued_; });
+        jobs_.push_back({std::move(path), std::move(rgba)});
+        work_.notify_one();
+    }
+    // Waits for every frame; returns the first error message ("" if none).
+    std::string finish()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            closing_ = true;
+        }
+        work_.notify_all();
+        for (auto &t : pool_)
+            if (t.joinable()) t.join();
+        pool_.clear();
+        return error_;
+    }
+
+  private:
+    struct Job {
+        std::string path;
+        std::vector<uint8_t> rgba;
+    };
+    void run()
+    {
+        for (;;) {
+            Job j;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                work_.wait(lk, [this] { return closing_ || !jobs_.empty(); });
+                if (jobs_.empty()) return;
+                j = std::move(jobs_.front());
+                jobs_.pop_front();
+                room_.notify_one();
+            }
+            std::string err;
+            if (!pfs::png::write_file(j.path, j.rgba.data(), w_, h_, err)) {
+                std::lock_guard<std::mutex> lk(mu_);
+                if (error_.empty()) error_ = err;
+            }
+        }
+    }
+    int w_, h_;
+    size_t max_queued_;
+    std::vector<std::thread> pool_;
+    std::deque<Job> jobs_;
+    std::mutex mu_;
+    std::condition_variable work_, room_;
+    bool closing_ = false;
+    std::string error_;
+};
 
 bool make_dir(const std::string &dir)
 {
@@ -130,23 +203,27 @@ int main(int argc, char *argv[])
 
     std::printf("Simulating [%d x %d] domain for %d timesteps at dt=%g...\n", velocity.height, velocity.width,
                 n_timesteps, (double)delta_t);
-    std::vector<uint8_t> bytes(image.size());
+    const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    PngWriters writers(input.width, input.height, write ? nthreads : 0, 2 * (size_t)nthreads);
     const auto t0 = std::chrono::high_resolution_clock::now();
     for (int i = 0; i < n_timesteps; ++i) {
         if (pfs_session_step(s, 1) != PFS_OK) return fail_api("pfs_session_step");
         if (write) {
             if (pfs_session_download(s, nullptr, nullptr, image.data(), PFS_HOST) != PFS_OK)
                 return fail_api("pfs_session_download");
+            std::vector<uint8_t> bytes(image.size());
             for (size_t k = 0; k < image.size(); ++k) bytes[k] = to_byte(image[k]);
-            const std::string path = std::string(argv[6]) + "/" + std::to_string(i) + ".png";
+            std::string path = std::string(argv[6]) + "/" + std::to_string(i) + ".png";
             std::printf("[%d] Writing to : %s\n", i, path.c_str());
-            if (!pfs::png::write_file(path, bytes.data(), input.width, input.height, err)) {
-                std::fprintf(stderr, "%s\n", err.c_str());
-                return 1;
-            }
+            writers.submit(std::move(path), std::move(bytes));
         }
     }
     if (pfs_session_sync(s) != PFS_OK) return fail_api("pfs_session_sync");
+    const std::string werr = writers.finish();  // every frame on disk before the clock stops
+    if (!werr.empty()) {
+        std::fprintf(stderr, "%s\n", werr.c_str());
+        return 1;
+    }
     const auto t1 = std::chrono::high_resolution_clock::now();
     std::printf("%d timesteps took %lld us.\n", n_timesteps,
                 (long long)std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count());

@@ -334,13 +334,9 @@ template <int G, int L>
 cudaError_t launch_ens(const EnsArgs &a, int grid, cudaStream_t st)
 {
     constexpr int smem = Ring<float, L>::bytes_per_block;
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_ensemble_step<G, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr_done{0};  // per instantiation and device
+    const cudaError_t ea = smem_limit_once(k_ensemble_step<G, L>, smem, attr_done);
+    if (ea != cudaSuccess) return ea;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(128);

@@ -22,6 +22,21 @@ inline cudaError_t launched(int n = 1)
     return cudaGetLastError();
 }
 
+// Raise a kernel's dynamic shared-memory limit once per device (function
+// attributes belong to a device's context); `done` holds one bit per device.
+template <typename F>
+inline cudaError_t smem_limit_once(F *kernel, int bytes, std::atomic<unsigned long long> &done)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_acq_rel);
+    return e;
+}
+
 // Reduction scratch: one double pair per block plus a ticket, so the last
 // block sums the partials in block order (deterministic result).
 struct Reduce {

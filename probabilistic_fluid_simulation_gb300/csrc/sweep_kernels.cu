@@ -56,13 +56,9 @@ template <typename T, int G, int L, bool PREV>
 cudaError_t launch_stream_t(const StreamArgs<T> &a, cudaStream_t st)
 {
     constexpr int smem = Ring<T, L>::bytes_per_block;
-    static bool attr_set = false;  // per instantiation; the attribute is per function
-    if (!attr_set) {
-        const cudaError_t e = cudaFuncSetAttribute(k_sweep_stream<T, G, L, PREV>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_done{0};  // per instantiation and device
+    const cudaError_t e = smem_limit_once(k_sweep_stream<T, G, L, PREV>, smem, attr_done);
+    if (e != cudaSuccess) return e;
     const int blocks = (a.nwork + 3) / 4;  // 4 warps per block: the shared rings are laid out for 4
     k_sweep_stream<T, G, L, PREV><<<blocks, 128, smem, st>>>(a);
     return launched();

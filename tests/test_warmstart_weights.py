@@ -10,7 +10,7 @@ def test_shipped_weights_layout_and_record():
     n = sum(co * 9 * R.cinp(ci) + co for ci, co in R.CONVS) + 17
     assert params.dtype == np.float32 and params.shape == (n,)
     assert np.isfinite(params).all()
-    assert meta["pairs"] == 20000 and meta["size"] == 256
+    assert meta["pairs"] == 40000 and meta["size"] == 256
     assert meta["training"]["val_loss"][-1] < 0.01
     assert WS.init_params(n).shape == params.shape
 
