@@ -95,11 +95,12 @@ def main():
     ap.add_argument("--chunk", type=int, default=32)
     ap.add_argument("--reps", type=int, default=100)
     ap.add_argument("--scan", action="store_true")
+    ap.add_argument("--scan-levels", default=",".join(str(x) for x in LEVELS), help="fuse depths for --scan")
     a = ap.parse_args()
     cells = a.size * (a.height or a.size)
     if a.scan:
         rows = []
-        for lv in LEVELS:
+        for lv in (int(x) for x in a.scan_levels.split(",")):
             for ch in CHUNKS:
                 us = time_sweeps(a.size, lv, ch, reps=a.reps, height=a.height)
                 rows.append({"levels": lv, "chunk": ch, "us_per_launch": us,
