@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the precision / batched form measurements")
     ap.add_argument("--form-size", type=int, default=4096)
     ap.add_argument("--form-steps", type=int, default=5)
+    ap.add_argument("--form-error-steps", type=int, default=100,
+                    help="steps of the per-field error run against the FP64 form (0: skip)")
     ap.add_argument("--members", type=int, default=512)
     ap.add_argument("--ens-steps", type=int, default=10)
     return ap.parse_args()
@@ -249,6 +251,57 @@ def precision_forms(a, fluid, synthetic, stream):
     for name, prec in (("plain_f32", fluid.PREC_F32), ("bf16", fluid.PREC_BF16), ("f16", fluid.PREC_F16),
                        ("f32r", fluid.PREC_F32R)):
         out[name] = time_session(fluid, vp, tmp, img, a.form_steps, stream, precision=prec, **kw)
+    if a.form_error_steps > 0:
+        out["fp64_error"] = precision_errors(a, fluid, vp, tmp, img, stream, kw)
+    return out
+
+
+def precision_errors(a, fluid, vp, tmp, img, stream, kw):
+    """Per-field error of each form against the FP64 form (the same method in
+    double) after the same number of steps from the same state: max |x - y| /
+    max |y| over the grid for u, v, p (the pressure), b (the divergence) and
+    the image. Every form runs the same sweep count per step when the cap
+    binds (it does at 4096x4096: Jacobi needs millions of sweeps there), so
+    the difference is rounding alone."""
+    import torch
+    n = vp.shape[0]
+    steps = a.form_error_steps
+
+    def run(prec):
+        vp64 = torch.empty((n, n, 4), dtype=torch.float64, device="cuda")
+        im64 = torch.empty(img.shape, dtype=torch.float64, device="cuda")
+        t0 = time.perf_counter()
+        with fluid.Session(n, n, image_shape=img.shape, stream=stream, precision=prec, **kw) as s:
+            s.upload(vp, tmp, img)
+            s.step(steps)
+            s.download_f64(vp64, im64)
+            s.sync()
+            st = s.stats()
+        return vp64, im64, time.perf_counter() - t0, st
+
+    ref_vp, ref_im, ref_s, ref_st = run(fluid.PREC_F64)
+    fields = ("u", "v", "p", "b", "image")
+    refs = [ref_vp[..., c] for c in range(4)] + [ref_im]
+    out = {"steps": steps, "measure": "max |x - x_fp64| / max |x_fp64| per field; rms: ||x - x_fp64|| / ||x_fp64||",
+           "note": "b is a near-cancelling difference of neighbouring velocities (the projected field is nearly "
+                   "divergence-free), so its relative error is the velocity error amplified by the cancellation, "
+                   "and p solves against b: O(1) for float32 storage too",
+           "fp64_run_s": round(ref_s, 2), "fp64_sweeps_last_step": ref_st["sweeps"]}
+    for name, prec in (("plain_f32", fluid.PREC_F32), ("bf16", fluid.PREC_BF16), ("f16", fluid.PREC_F16),
+                       ("f32r", fluid.PREC_F32R)):
+        x_vp, x_im, _, st = run(prec)
+        xs = [x_vp[..., c] for c in range(4)] + [x_im]
+        e = {}
+        for f, x, y in zip(fields, xs, refs):
+            m, nrm = float(y.abs().max()), float(y.norm())
+            d = x - y
+            e[f] = float(d.abs().max()) / m if m > 0 else float(d.abs().max())
+            e["rms_" + f] = float(d.norm()) / nrm if nrm > 0 else float(d.norm())
+        e["sweeps_last_step"] = st["sweeps"]
+        out[name] = e
+        del x_vp, x_im, xs
+    del ref_vp, ref_im, refs
+    torch.cuda.empty_cache()
     return out
 
 

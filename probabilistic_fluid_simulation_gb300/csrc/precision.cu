@@ -216,7 +216,10 @@ __global__ void k_lp_scale(const float *__restrict__ r, T *__restrict__ rt, size
         rt[k] = Store<T>::from_f(r[k] * s);
 }
 
-// FP64 form: one Jacobi sweep (src/fluid.cpp:239-257 in double).
+// FP64 form: one Jacobi sweep (src/fluid.cpp:239-257 in double). The
+// division by 4 is a multiplication by 0.25: both are the correctly rounded
+// value of the same exact quotient (4 is a power of two), so the bits are
+// those of the division, without FP64 division's iteration.
 __global__ void k_f64_sweep(const double *__restrict__ pin, const double *__restrict__ b, double *__restrict__ pout,
                             int ld, int w, int h)
 {
@@ -226,7 +229,7 @@ __global__ void k_f64_sweep(const double *__restrict__ pin, const double *__rest
     const double s = __dadd_rn(__dadd_rn(__dadd_rn(pin[r + wm_(i, w)], pin[r + wp_(i, w)]),
                                          pin[(size_t)wm_(j, h) * ld + i]),
                                pin[(size_t)wp_(j, h) * ld + i]);
-    pout[r + i] = __ddiv_rn(__dadd_rn(s, b[r + i]), 4.0);
+    pout[r + i] = __dmul_rn(__dadd_rn(s, b[r + i]), 0.25);
 }
 
 // Damped Jacobi pass on a predicted start, in FP64: x_out = x + (b - A x) / 8,
