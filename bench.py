@@ -616,32 +616,58 @@ def main():
                 "traffic_source": tsrc}
     del p, bpl, q
 
-    # e2e: the same steps through the C ABI with pinned host buffers in and out each step
+    # e2e: the same steps through the C ABI, every step's state copied in from pinned host buffers
+    # and its result (both velocity buffers and the image) copied back out
     e2e = None
     if not a.no_e2e:
         ne = a.e2e_steps or a.steps
-        hv = torch.from_numpy(vp.copy()).pin_memory().numpy()
-        ht = torch.from_numpy(np.zeros_like(tmp)).pin_memory().numpy()
-        hi = torch.from_numpy(img.copy()).pin_memory().numpy()
-        sess.upload(hv, ht, hi)
+
+        def pinned(x):
+            return torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()
+        hin = (pinned(vp), pinned(np.zeros_like(tmp)), pinned(img))
+        hout = tuple(pinned(np.zeros_like(x)) for x in hin)
+
+        def timed(fn):
+            if dist:
+                dist.barrier()
+            t0 = time.perf_counter()
+            fn()
+            el = time.perf_counter() - t0
+            if dist:
+                t = torch.tensor([el], device="cuda", dtype=torch.float64)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                el = float(t.item())
+            return el
+
+        def serial():  # each call returns once its copy is done
+            for _ in range(ne):
+                sess.upload(*hin)
+                sess.step(1)
+                sess.download(*hout)
+
+        def pipelined():  # the next state's upload is queued before each step: copies overlap the steps
+            sess.upload_async(*hin)
+            for k in range(ne):
+                if k + 1 < ne:
+                    sess.upload_async(*hin)
+                sess.step(1)
+                sess.download_async(*hout)
+            sess.sync()
+
+        sess.upload(*hin)
         sess.step(1)
-        sess.download(hv, ht, hi)
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(ne):
-            sess.upload(hv, ht, hi)
-            sess.step(1)
-            sess.download(hv, ht, hi)
-        el = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([el], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
-        nbytes = hv.nbytes + ht.nbytes + hi.nbytes
+        sess.download(*hout)
+        el_serial = timed(serial)
+        pipelined()
+        el = timed(pipelined)
+        nbytes = sum(x.nbytes for x in hin)
         e2e = {"value": cells * ne * world / el, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "steps": ne,
-               "api": "pfs_session_upload(PFS_HOST) + pfs_session_step(1) + pfs_session_download(PFS_HOST)"}
+               "d2h_bytes_per_step": sum(x.nbytes for x in hout), "steps": ne,
+               "api": "pfs_session_upload_async + pfs_session_step(1) + pfs_session_download_async per step, "
+                      "pinned host buffers, pfs_session_sync at the end",
+               "serial": {"value": cells * ne * world / el_serial,
+                          "api": "pfs_session_upload(PFS_HOST) + pfs_session_step(1) + "
+                                 "pfs_session_download(PFS_HOST) per step"}}
     sess.close()
 
     forms = None

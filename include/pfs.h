@@ -218,8 +218,42 @@ int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, in
  * image. For the F32 form the pressure is the final iterate (tmp's channel 2). */
 int pfs_session_download_f64(pfs_session *s, double *vp, double *image, int where);
 int pfs_session_stats(pfs_session *s, pfs_stats *out);
+/* Waits for the steps and for the asynchronous transfers queued so far. */
 int pfs_session_sync(pfs_session *s);
 int pfs_session_destroy(pfs_session *s);
+
+/* ---- asynchronous host transfers ------------------------------------------------------ */
+/*
+ * For a stream of states in and results out, with the copies running on the
+ * session's own copy streams beside the steps (the reference's CLI declares
+ * NUM_STREAMS for this and never uses it, src/main.cpp:30,198-200). Host
+ * buffers should be pinned (page-locked): pageable ones work, but their copies
+ * cannot overlap the steps.
+ *
+ * pfs_session_upload_async queues a state, host buffers laid out as for
+ * pfs_session_upload. Its host-to-device copy starts at once; the state
+ * replaces the session's state when the next pfs_session_step begins (each
+ * pfs_session_step call takes the oldest queued state, if any). At most
+ * PFS_IO_SLOTS states can be queued; one more returns
+ * PFS_ERR_INVALID_ARGUMENT. The buffers must stay unchanged until
+ * pfs_session_wait_io or pfs_session_sync returns.
+ *
+ * pfs_session_download_async queues a copy of the state as it stands after
+ * the steps queued so far into host buffers (any may be NULL), laid out as
+ * for pfs_session_download, and returns at once; the buffers hold the result
+ * when pfs_session_wait_io or pfs_session_sync returns. Up to PFS_IO_SLOTS
+ * downloads are in flight; a further one makes the device (not the host)
+ * wait for the oldest.
+ *
+ * pfs_session_wait_io waits for every transfer queued so far, not for steps
+ * queued after them. Downloads of any kind read the state as it stands,
+ * whatever uploads are queued; pfs_session_upload returns
+ * PFS_ERR_INVALID_ARGUMENT while a queued upload has not been taken by a step.
+ */
+enum { PFS_IO_SLOTS = 2 };
+int pfs_session_upload_async(pfs_session *s, const float *vp, const float *tmp, const float *image);
+int pfs_session_download_async(pfs_session *s, float *vp, float *tmp, float *image);
+int pfs_session_wait_io(pfs_session *s);
 
 /* ---- learned warm start -------------------------------------------------------------- */
 /*

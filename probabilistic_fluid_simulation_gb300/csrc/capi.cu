@@ -530,13 +530,34 @@ struct pfs_session {
     int start_mode = PFS_START_PREVIOUS;
     pfs::unet::Net *net = nullptr;
     int net_coarsen = 1, net_passes = 1;
+    // asynchronous host transfers: two device staging slots each way, copies on
+    // the session's own copy streams, ordered against the compute stream by events
+    struct IoSlot {
+        float *buf = nullptr;
+        cudaEvent_t copied = nullptr;  // upload: host-to-device copy done; download: device-to-host copy done
+        cudaEvent_t used = nullptr;    // upload: split into the state done; download: merge into buf done
+    };
+    IoSlot up[PFS_IO_SLOTS], down[PFS_IO_SLOTS];
+    cudaStream_t up_st = nullptr, down_st = nullptr;
+    int up_head = 0, up_count = 0, down_next = 0;
+    size_t io_floats = 0;  // floats per slot: vp, tmp, image
     ~pfs_session()
     {
+        if (up_st) cudaStreamSynchronize(up_st);
+        if (down_st) cudaStreamSynchronize(down_st);
+        for (IoSlot *k : {&up[0], &up[1], &down[0], &down[1]}) {
+            if (k->buf) cudaFree(k->buf);
+            if (k->copied) cudaEventDestroy(k->copied);
+            if (k->used) cudaEventDestroy(k->used);
+        }
+        if (up_st) cudaStreamDestroy(up_st);
+        if (down_st) cudaStreamDestroy(down_st);
         if (img_mem) cudaFree(img_mem);
         if (stage) cudaFree(stage);
         if (lp) pfs::lp_destroy(lp);
     }
 };
+static_assert(PFS_IO_SLOTS == 2, "the slot destructor loop lists two slots each way");
 
 extern "C" {
 
@@ -836,10 +857,58 @@ static int session_stage(pfs_session *s, size_t bytes)
     return PFS_OK;
 }
 
+// The state from interleaved device buffers (vp, tmp, image), queued on the
+// session stream.
+static int apply_state(pfs_session *s, const float *A, const float *B, const float *I)
+{
+    if (s->lp) return pfs::lp_upload(s->lp, A, B, I, s->st);
+    Field &f = s->f;
+    f.pidx[0] = 0;
+    f.pidx[1] = 1;
+    s->vpSlot = 0;
+    s->tmpSlot = 1;
+    CK(pfs::launch_split_vp(A, f.u[0], f.v[0], f.p[0], f.b, f.ld, f.w, f.h, s->st));
+    CK(pfs::launch_split_vp(B, f.u[1], f.v[1], f.p[1], nullptr, f.ld, f.w, f.h, s->st));
+    if (s->ic > 0) {
+        s->icur = 0;
+        CK(pfs::launch_split_image(I, s->img[0], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
+    }
+    return PFS_OK;
+}
+
+// The state into interleaved device buffers (any of them null: skipped), in
+// the reference's layout, queued on the session stream.
+static int merge_state(pfs_session *s, float *A, float *B, float *I)
+{
+    if (s->lp) {
+        // (u, v, final pressure, divergence) into both velocity buffers
+        if (A) CKS(pfs::lp_download(s->lp, A, I, s->st));
+        if (B) CKS(pfs::lp_download(s->lp, B, A ? nullptr : I, s->st));
+        if (!A && !B && I) CKS(pfs::lp_download(s->lp, nullptr, I, s->st));
+        return PFS_OK;
+    }
+    Field &f = s->f;
+    const int W = s->vpSlot, Z = s->tmpSlot;
+    if (A) CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, f.w, f.h, s->st));
+    if (B) CK(pfs::launch_merge_velocity(B, f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.b, f.ld, f.w, f.h, s->st));
+    if (I && s->ic > 0) CK(pfs::launch_merge_image(I, s->img[s->icur], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
+    return PFS_OK;
+}
+
+// A synchronous upload is refused while asynchronous ones wait for a step:
+// the next step would replace its state by the oldest of them.
+static int no_queued_upload(pfs_session *s)
+{
+    if (s->up_count > 0)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "an asynchronous upload is queued: step the session first");
+    return PFS_OK;
+}
+
 int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const float *image, int where)
 {
     if (!s || !vp || !tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
     if (s->ic > 0 && !image) return fail(PFS_ERR_INVALID_ARGUMENT, "session has an image: pass it");
+    CKS(no_queued_upload(s));
     Field &f = s->f;
     const size_t vcount = (size_t)f.w * f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
     const float *A = vp, *B = tmp, *I = image;
@@ -858,28 +927,96 @@ int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const 
         CKS(check_aligned(vp, "vp"));
         CKS(check_aligned(tmp, "tmp"));
     }
-    if (s->lp) {
-        CKS(pfs::lp_upload(s->lp, A, B, I, s->st));
-        if (where == PFS_HOST) CK(cudaStreamSynchronize(s->st));
-        return PFS_OK;
-    }
-    f.pidx[0] = 0;
-    f.pidx[1] = 1;
-    s->vpSlot = 0;
-    s->tmpSlot = 1;
-    CK(pfs::launch_split_vp(A, f.u[0], f.v[0], f.p[0], f.b, f.ld, f.w, f.h, s->st));
-    CK(pfs::launch_split_vp(B, f.u[1], f.v[1], f.p[1], nullptr, f.ld, f.w, f.h, s->st));
-    if (s->ic > 0) {
-        s->icur = 0;
-        CK(pfs::launch_split_image(I, s->img[0], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
-    }
+    CKS(apply_state(s, A, B, I));
     if (where == PFS_HOST) CK(cudaStreamSynchronize(s->st));
+    return PFS_OK;
+}
+
+// Copy streams, events and the staging slots of the asynchronous transfers,
+// made on first use.
+static int io_init(pfs_session *s)
+{
+    if (s->up_st) return PFS_OK;
+    const size_t vcount = (size_t)s->f.w * s->f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
+    s->io_floats = 2 * vcount + icount;
+    for (pfs_session::IoSlot *k : {&s->up[0], &s->up[1], &s->down[0], &s->down[1]}) {
+        CK(cudaMalloc(&k->buf, s->io_floats * sizeof(float)));
+        CK(cudaEventCreateWithFlags(&k->copied, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&k->used, cudaEventDisableTiming));
+    }
+    CK(cudaStreamCreateWithFlags(&s->down_st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&s->up_st, cudaStreamNonBlocking));
+    return PFS_OK;
+}
+
+int pfs_session_upload_async(pfs_session *s, const float *vp, const float *tmp, const float *image)
+{
+    if (!s || !vp || !tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
+    if (s->ic > 0 && !image) return fail(PFS_ERR_INVALID_ARGUMENT, "session has an image: pass it");
+    if (s->up_count == PFS_IO_SLOTS)
+        return fail(PFS_ERR_INVALID_ARGUMENT, "%d asynchronous uploads are queued already", PFS_IO_SLOTS);
+    CKS(io_init(s));
+    const size_t vcount = (size_t)s->f.w * s->f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
+    pfs_session::IoSlot &k = s->up[(s->up_head + s->up_count) % PFS_IO_SLOTS];
+    // the slot's previous contents must have been split into the state (no wait before the first use)
+    CK(cudaStreamWaitEvent(s->up_st, k.used, 0));
+    CK(cudaMemcpyAsync(k.buf, vp, vcount * sizeof(float), cudaMemcpyHostToDevice, s->up_st));
+    CK(cudaMemcpyAsync(k.buf + vcount, tmp, vcount * sizeof(float), cudaMemcpyHostToDevice, s->up_st));
+    if (icount)
+        CK(cudaMemcpyAsync(k.buf + 2 * vcount, image, icount * sizeof(float), cudaMemcpyHostToDevice, s->up_st));
+    CK(cudaEventRecord(k.copied, s->up_st));
+    s->up_count++;
+    return PFS_OK;
+}
+
+// The oldest queued upload becomes the state (queued on the session stream
+// behind its copy).
+static int apply_queued_upload(pfs_session *s)
+{
+    if (s->up_count == 0) return PFS_OK;
+    const size_t vcount = (size_t)s->f.w * s->f.h * 4;
+    pfs_session::IoSlot &k = s->up[s->up_head];
+    CK(cudaStreamWaitEvent(s->st, k.copied, 0));
+    CKS(apply_state(s, k.buf, k.buf + vcount, k.buf + 2 * vcount));
+    CK(cudaEventRecord(k.used, s->st));
+    s->up_head = (s->up_head + 1) % PFS_IO_SLOTS;
+    s->up_count--;
+    return PFS_OK;
+}
+
+int pfs_session_download_async(pfs_session *s, float *vp, float *tmp, float *image)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    CKS(io_init(s));
+    const size_t vcount = (size_t)s->f.w * s->f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
+    pfs_session::IoSlot &k = s->down[s->down_next];
+    s->down_next = (s->down_next + 1) % PFS_IO_SLOTS;
+    // the slot's previous contents must have reached the host before the merge overwrites them
+    CK(cudaStreamWaitEvent(s->st, k.copied, 0));
+    float *A = vp ? k.buf : nullptr, *B = tmp ? k.buf + vcount : nullptr;
+    float *I = (image && icount) ? k.buf + 2 * vcount : nullptr;
+    CKS(merge_state(s, A, B, I));
+    CK(cudaEventRecord(k.used, s->st));
+    CK(cudaStreamWaitEvent(s->down_st, k.used, 0));
+    if (A) CK(cudaMemcpyAsync(vp, A, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->down_st));
+    if (B) CK(cudaMemcpyAsync(tmp, B, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->down_st));
+    if (I) CK(cudaMemcpyAsync(image, I, icount * sizeof(float), cudaMemcpyDeviceToHost, s->down_st));
+    CK(cudaEventRecord(k.copied, s->down_st));
+    return PFS_OK;
+}
+
+int pfs_session_wait_io(pfs_session *s)
+{
+    if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
+    if (s->up_st) CK(cudaStreamSynchronize(s->up_st));
+    if (s->down_st) CK(cudaStreamSynchronize(s->down_st));
     return PFS_OK;
 }
 
 int pfs_session_step(pfs_session *s, int n)
 {
     if (!s || n < 0) return fail(PFS_ERR_INVALID_ARGUMENT, "bad session or step count");
+    if (n > 0) CKS(apply_queued_upload(s));
     if (s->lp) {
         pfs::LpParams lp;
         lp.dt = s->prm.dt;
@@ -992,18 +1129,7 @@ int pfs_session_download(pfs_session *s, float *vp, float *tmp, float *image, in
         if (vp) CKS(check_aligned(vp, "vp"));
         if (tmp) CKS(check_aligned(tmp, "tmp"));
     }
-    const int W = s->vpSlot, Z = s->tmpSlot;
-    if (s->lp) {
-        // (u, v, final pressure, divergence) into both velocity buffers
-        if (A) CKS(pfs::lp_download(s->lp, A, I, s->st));
-        if (B) CKS(pfs::lp_download(s->lp, B, A ? nullptr : I, s->st));
-        if (!A && !B && I) CKS(pfs::lp_download(s->lp, nullptr, I, s->st));
-    } else {
-        if (A) CK(pfs::launch_merge_velocity(A, f.u[W], f.v[W], f.p[f.pidx[W]], f.b, f.ld, f.w, f.h, s->st));
-        if (B) CK(pfs::launch_merge_velocity(B, f.u[Z], f.v[Z], f.p[f.pidx[Z]], f.b, f.ld, f.w, f.h, s->st));
-        if (I && s->ic > 0)
-            CK(pfs::launch_merge_image(I, s->img[s->icur], s->iplane, s->ild, s->iw, s->ih, s->ic, s->st));
-    }
+    CKS(merge_state(s, A, B, I));
     if (where == PFS_HOST) {
         if (vp) CK(cudaMemcpyAsync(vp, A, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
         if (tmp) CK(cudaMemcpyAsync(tmp, B, vcount * sizeof(float), cudaMemcpyDeviceToHost, s->st));
@@ -1060,7 +1186,7 @@ int pfs_session_sync(pfs_session *s)
 {
     if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
     CK(cudaStreamSynchronize(s->st));
-    return PFS_OK;
+    return pfs_session_wait_io(s);
 }
 
 int pfs_session_destroy(pfs_session *s)

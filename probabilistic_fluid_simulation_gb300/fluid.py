@@ -95,6 +95,9 @@ SIGNATURES = [
     ("pfs_session_download_f64", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("pfs_session_stats", C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     ("pfs_session_sync", C.c_int, [C.c_void_p]),
+    ("pfs_session_upload_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("pfs_session_download_async", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("pfs_session_wait_io", C.c_int, [C.c_void_p]),
     ("pfs_session_destroy", C.c_int, [C.c_void_p]),
     ("pfs_unet_create", C.c_int, [C.POINTER(C.c_void_p), C.c_longlong]),
     ("pfs_unet_destroy", C.c_int, [C.c_void_p]),
@@ -332,13 +335,53 @@ class Session:
         else:
             _check(lib().pfs_session_set_start(self._h, int(mode), net._h if net is not None else None))
 
+    def upload_async(self, vp: np.ndarray, tmp: np.ndarray, image: Optional[np.ndarray] = None):
+        """Queue a state from host arrays (pinned ones overlap the copy with
+        the steps); the next step() starts from it. The arrays are kept
+        referenced, and must stay unchanged, until wait_io() or sync()."""
+        self._check_host(vp, tmp, image, "upload_async")
+        _check(lib().pfs_session_upload_async(self._h, C.c_void_p(_ptr(vp)), C.c_void_p(_ptr(tmp)),
+                                              C.c_void_p(_ptr(image) if image is not None else None)))
+        self._inflight().append((vp, tmp, image))
+
+    def download_async(self, vp: Optional[np.ndarray] = None, tmp: Optional[np.ndarray] = None,
+                       image: Optional[np.ndarray] = None):
+        """Queue a copy of the state after the steps queued so far into host
+        arrays; they hold it once wait_io() or sync() has returned."""
+        self._check_host(vp, tmp, image, "download_async")
+        _check(lib().pfs_session_download_async(self._h, C.c_void_p(_ptr(vp) if vp is not None else None),
+                                                C.c_void_p(_ptr(tmp) if tmp is not None else None),
+                                                C.c_void_p(_ptr(image) if image is not None else None)))
+        self._inflight().append((vp, tmp, image))
+
+    def _check_host(self, vp, tmp, image, what):
+        ih, iw, ic = self.image_shape
+        for a, n in ((vp, self.h * self.w * 4), (tmp, self.h * self.w * 4), (image, ih * iw * ic)):
+            if a is None:
+                continue
+            if not isinstance(a, np.ndarray):
+                raise TypeError(f"{what} takes host (numpy) arrays")
+            if a.size != n:
+                raise ValueError(f"{what}: buffer of {a.size} floats, {n} expected")
+
+    def _inflight(self) -> list:
+        if not hasattr(self, "_io"):
+            self._io = []
+        return self._io
+
+    def wait_io(self):
+        _check(lib().pfs_session_wait_io(self._h))
+        self._inflight().clear()
+
     def sync(self):
         _check(lib().pfs_session_sync(self._h))
+        self._inflight().clear()
 
     def close(self):
         if self._h:
             lib().pfs_session_destroy(self._h)
             self._h = C.c_void_p()
+        self._inflight().clear()
 
     def __del__(self):
         try:
