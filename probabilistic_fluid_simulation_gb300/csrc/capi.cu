@@ -88,9 +88,11 @@ struct Field {
     int pidx[2] = {0, 1};  // pressure plane holding channel 2 of velocity slot 0 / 1
     double *rmem = nullptr;
     unsigned *ticket = nullptr;
-    double *hres = nullptr;  // pinned, [2]
+    double *hres = nullptr;  // pinned and mapped, [2]
+    double *hres_d = nullptr;           // its device alias
     pfs::SolveState *dstate = nullptr;  // device
-    pfs::SolveState *hstate = nullptr;  // pinned host copy
+    pfs::SolveState *hstate = nullptr;  // pinned and mapped host copy
+    pfs::SolveState *hstate_d = nullptr;
     float *pback = nullptr;             // plain start kept aside while a predicted start is tried
     float *pnet = nullptr;              // the network's correction in the later passes of a predicted start
     Reduce red{};
@@ -131,10 +133,13 @@ struct Field {
         CK(cudaMalloc(&rmem, (2 * nb + 2) * sizeof(double) + 16));
         CK(cudaMemset(rmem, 0, (2 * nb + 2) * sizeof(double) + 16));
         ticket = reinterpret_cast<unsigned *>(rmem + 2 * nb + 2);
-        CK(cudaMallocHost(&hres, 2 * sizeof(double)));
+        // host copies of the check results: mapped, written by a kernel (launch_copy_small)
+        CK(cudaHostAlloc(&hres, 2 * sizeof(double), cudaHostAllocMapped));
+        CK(cudaHostGetDevicePointer((void **)&hres_d, hres, 0));
         CK(cudaMalloc(&dstate, sizeof(pfs::SolveState)));
         CK(cudaMemset(dstate, 0, sizeof(pfs::SolveState)));
-        CK(cudaMallocHost(&hstate, sizeof(pfs::SolveState)));
+        CK(cudaHostAlloc(&hstate, sizeof(pfs::SolveState), cudaHostAllocMapped));
+        CK(cudaHostGetDevicePointer((void **)&hstate_d, hstate, 0));
         red.partials = rmem;
         red.result = rmem + 2 * nb;
         red.ticket = ticket;
@@ -201,7 +206,7 @@ bool fused_ok(const Field &f) { return f.w % 4 == 0; }
 int residual_host(Field &f, const float *pp, cudaStream_t st, double &rr, double &bb)
 {
     CK(pfs::launch_residual(pp, f.b, f.ld, f.w, f.h, f.red, nullptr, 0, 0.0, st));
-    CK(cudaMemcpyAsync(f.hres, f.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(pfs::launch_copy_small(f.red.result, f.hres_d, 2 * sizeof(double), st));
     CK(cudaStreamSynchronize(st));
     rr = f.hres[0];
     bb = f.hres[1];
@@ -242,7 +247,7 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     const int L = std::max(1, std::min(c.tun.levels, c.tun.halo));
     const bool resid = c.tol > 0.0;
     const int *done = resid ? &f.dstate->done : nullptr;
-    if (resid) CK(cudaMemsetAsync(f.dstate, 0, sizeof(pfs::SolveState), st));
+    if (resid) CK(pfs::launch_zero_small(f.dstate, sizeof(pfs::SolveState), st));
     if (resid) CKS(f.make_aux());
     bool pending = false;  // a residual launch on f.aux that st has not waited for
     int since = 0;         // sweep launches since the last check
@@ -295,7 +300,7 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
         marks[nmarks++] = {S, cur, prev};
         if (++in_batch == batch || S == c.S || nmarks == 64 || watch) {
             CKS(settle());
-            CK(cudaMemcpyAsync(f.hstate, f.dstate, sizeof(pfs::SolveState), cudaMemcpyDeviceToHost, st));
+            CK(pfs::launch_copy_small(f.dstate, f.hstate_d, sizeof(pfs::SolveState), st));
             CK(cudaStreamSynchronize(st));
             if (f.hstate->done || S == c.S) finished = true;
             if (watch && !finished && o.start_kind == PFS_START_NETWORK) {

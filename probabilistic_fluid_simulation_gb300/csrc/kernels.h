@@ -104,6 +104,13 @@ cudaError_t launch_damp(const float *pin, const float *b, float *pout, int ld, i
 // r = b - A p (float, per cell) and p += d: the later passes of a predicted start
 cudaError_t launch_residual_field(const float *p, const float *b, float *r, int ld, int w, int h, cudaStream_t st);
 cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st);
+// Small transfers (bytes a multiple of 4, at most 1 MiB, 4-byte aligned) run
+// as a one-warp kernel instead of a copy-engine operation, so they never
+// queue behind bulk copies that occupy the copy engines (asynchronous session
+// transfers). dst may be device memory or the device alias of mapped pinned
+// host memory.
+cudaError_t launch_copy_small(const void *src, void *dst, size_t bytes, cudaStream_t st);
+cudaError_t launch_zero_small(void *dst, size_t bytes, cudaStream_t st);
 
 // ---- pressure (sweep_kernels.cu, residual_kernels.cu) ----
 int stream_strip_width(int halo);

@@ -399,7 +399,8 @@ struct LpState {
     double *rmem = nullptr;
     unsigned *maxabs = nullptr;
     double *escale = nullptr;
-    double *hres = nullptr;
+    double *hres = nullptr;    // pinned and mapped: written by launch_copy_small
+    double *hres_d = nullptr;  // its device alias
     Reduce red{};
     void *stage = nullptr;
     size_t stage_bytes = 0;
@@ -441,11 +442,11 @@ double rel_of(double rr, double bb) { return bb > 0.0 ? std::sqrt(rr) / std::sqr
 template <typename T>
 int lp_residual(LpState &s, const double *x, double *xo, cudaStream_t st, double &rel)
 {
-    LCK(cudaMemsetAsync(s.maxabs, 0, sizeof(unsigned), st));
+    LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
     k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(x, (const T *)nullptr, s.escale, (const float *)s.b, xo, s.r, s.ld,
                                                    s.w, s.h, s.red, s.maxabs);
     LCK(launched());
-    LCK(cudaMemcpyAsync(s.hres, s.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
     LCK(cudaStreamSynchronize(st));
     rel = rel_of(s.hres[0], s.hres[1]);
     return PFS_OK;
@@ -540,12 +541,12 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
     o.checks = 0;
     for (;;) {
         // x_new = x + e/scale; r = b - A x_new (FP64); |r| stats
-        LCK(cudaMemsetAsync(s.maxabs, 0, sizeof(unsigned), st));
+        LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
         k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], ecur, s.escale, (const float *)s.b,
                                                        s.x[1 - s.xcur], s.r, ld, w, h, s.red, s.maxabs);
         LCK(launched());
         s.xcur = 1 - s.xcur;
-        LCK(cudaMemcpyAsync(s.hres, s.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
         LCK(cudaStreamSynchronize(st));
         o.checks++;
         o.rel = rel_of(s.hres[0], s.hres[1]);
@@ -607,7 +608,7 @@ int lp_step64(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
         if (!resid) break;
         k_f64_residual<<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], (double *)s.b, ld, w, h, s.red);
         LCK(launched());
-        LCK(cudaMemcpyAsync(s.hres, s.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
         LCK(cudaStreamSynchronize(st));
         o.checks++;
         o.rel = rel_of(s.hres[0], s.hres[1]);
@@ -712,7 +713,8 @@ int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
     const size_t rbytes = (2 * nb + 3) * sizeof(double) + 16;
     e = cudaMalloc(&s->rmem, rbytes);
     if (e == cudaSuccess) e = cudaMemset(s->rmem, 0, rbytes);
-    if (e == cudaSuccess) e = cudaMallocHost(&s->hres, 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaHostAlloc(&s->hres, 2 * sizeof(double), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->hres_d, s->hres, 0);
     if (e != cudaSuccess) {
         lp_destroy(s);
         return lp_fail(PFS_ERR_CUDA, cudaGetErrorString(e));

@@ -305,6 +305,27 @@ cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
     return launched();
 }
 
+// A few words copied (src non-null) or zeroed by one warp; stores to mapped
+// host memory are made visible to the host before the kernel completes.
+__global__ void k_small_words(const unsigned *__restrict__ src, unsigned *__restrict__ dst, int words)
+{
+    for (int k = threadIdx.x; k < words; k += 32) dst[k] = src ? src[k] : 0u;
+    __threadfence_system();
+}
+
+cudaError_t launch_copy_small(const void *src, void *dst, size_t bytes, cudaStream_t st)
+{
+    if (bytes % 4 != 0 || bytes > (1u << 20)) return cudaErrorInvalidValue;
+    k_small_words<<<1, 32, 0, st>>>(static_cast<const unsigned *>(src), static_cast<unsigned *>(dst),
+                                    (int)(bytes / 4));
+    return launched();
+}
+
+cudaError_t launch_zero_small(void *dst, size_t bytes, cudaStream_t st)
+{
+    return launch_copy_small(nullptr, dst, bytes, st);
+}
+
 #define PFS_BC_DISPATCH(bc, KERNEL, GRID, ...)                                     \
     do {                                                                           \
         switch (bc) {                                                              \
