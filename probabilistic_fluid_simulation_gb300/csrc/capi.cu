@@ -96,6 +96,10 @@ struct Field {
     float *pback = nullptr;             // plain start kept aside while a predicted start is tried
     float *pnet = nullptr;              // the network's correction in the later passes of a predicted start
     Reduce red{};
+    // the fused check launches (one block per 4 sweep warp tasks): own partials,
+    // red's result and tickets
+    double *psweep = nullptr;
+    Reduce red_sweep{};
     // residual checks run here, overlapping the sweep launch that follows them
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_check = nullptr, ev_res = nullptr;
@@ -144,12 +148,20 @@ struct Field {
         red.result = rmem + 2 * nb;
         red.ticket = ticket;
         red.nblocks = nb;
+        // capacity for the fused check launches at chunks of 16 rows or more
+        const int ns = std::max(nb, pfs::sweep_stream_blocks(w, h, 16));
+        CK(cudaMalloc(&psweep, 2 * (size_t)ns * sizeof(double)));
+        red_sweep = red;
+        red_sweep.partials = psweep;
+        red_sweep.nblocks = ns;
         return PFS_OK;
     }
     void release()
     {
         if (mem) cudaFree(mem);
         if (rmem) cudaFree(rmem);
+        if (psweep) cudaFree(psweep);
+        psweep = nullptr;
         if (hres) cudaFreeHost(hres);
         if (dstate) cudaFree(dstate);
         if (hstate) cudaFreeHost(hstate);
@@ -231,13 +243,17 @@ struct CheckPoint {
 // batches that double in size (1, 2, 4, ...) and reads the state only between
 // batches, then takes the plane roles recorded at the converged check point.
 //
-// The residual launch runs on the field's second stream and overlaps the
-// sweep launch that follows it: that launch reads q_S and b, as the residual
-// does, and writes only the third plane. The launch after it (which
-// overwrites q_S or q_{S-1}), any launch writing the q_{S-1} plane, the
-// host's reads of the state and the end of the solve wait for the residual.
-// If the check turns out converged, the one launch that ran meanwhile has
-// written only the plane no role refers to.
+// With the fused sweep (width a multiple of 4) the last launch of each check
+// interval evaluates the exact residual of its output itself
+// (launch_sweep_stream_check: fused levels <= 7, so an interval's last
+// 8-level launch is split 4 + 4): no second pass over p and b. Otherwise the
+// residual launch runs on the field's second stream and overlaps the sweep
+// launch that follows it: that launch reads q_S and b, as the residual does,
+// and writes only the third plane. The launch after it (which overwrites q_S
+// or q_{S-1}), any launch writing the q_{S-1} plane, the host's reads of the
+// state and the end of the solve wait for the residual. If the check turns
+// out converged, the one launch that ran meanwhile has written only the plane
+// no role refers to.
 int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStream_t st, int &cur, int &prev)
 {
     cur = f.pidx[X];
@@ -246,6 +262,9 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     const bool fused = fused_ok(f);
     const int L = std::max(1, std::min(c.tun.levels, c.tun.halo));
     const bool resid = c.tol > 0.0;
+    // the last fused launch of each check interval evaluates the residual itself
+    const bool check_fused =
+        fused && resid && pfs::sweep_stream_blocks(f.w, f.h, c.tun.chunk) <= f.red_sweep.nblocks;
     const int *done = resid ? &f.dstate->done : nullptr;
     if (resid) CK(pfs::launch_zero_small(f.dstate, sizeof(pfs::SolveState), st));
     if (resid) CKS(f.make_aux());
@@ -279,11 +298,19 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
                 S += 1;
                 continue;
             }
-            const int n = std::min(L, stop - S);
-            const bool last = (S + n == stop);
+            int n = std::min(L, stop - S);
+            bool last = (S + n == stop);
+            if (check_fused && last && n == 8) {  // the check launch fuses at most 7 levels: 8 = 4 + 4
+                n = 4;
+                last = false;
+            }
             if (pending && (since >= 1 || last)) CKS(settle());
-            CK(pfs::launch_sweep_stream(f.p[cur], f.b, f.p[freep], last ? f.p[prev] : nullptr, f.ld, f.w, f.h, n,
-                                        c.tun.halo, c.tun.chunk, done, st));
+            if (check_fused && last)
+                CK(pfs::launch_sweep_stream_check(f.p[cur], f.b, f.p[freep], f.p[prev], f.ld, f.w, f.h, n,
+                                                  c.tun.chunk, f.red_sweep, f.dstate, S + n, c.tol, done, st));
+            else
+                CK(pfs::launch_sweep_stream(f.p[cur], f.b, f.p[freep], last ? f.p[prev] : nullptr, f.ld, f.w, f.h,
+                                            n, c.tun.halo, c.tun.chunk, done, st));
             ++since;
             const int old_cur = cur;
             cur = freep;  // q_S; after a `last` launch prev holds q_{S-1}
@@ -291,12 +318,14 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
             S += n;
         }
         if (!resid) break;
-        CK(cudaEventRecord(f.ev_check, st));
-        CK(cudaStreamWaitEvent(f.aux, f.ev_check, 0));
-        CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, f.aux));
-        CK(cudaEventRecord(f.ev_res, f.aux));
-        pending = true;
-        since = 0;
+        if (!check_fused) {
+            CK(cudaEventRecord(f.ev_check, st));
+            CK(cudaStreamWaitEvent(f.aux, f.ev_check, 0));
+            CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, f.aux));
+            CK(cudaEventRecord(f.ev_res, f.aux));
+            pending = true;
+            since = 0;
+        }
         marks[nmarks++] = {S, cur, prev};
         if (++in_batch == batch || S == c.S || nmarks == 64 || watch) {
             CKS(settle());

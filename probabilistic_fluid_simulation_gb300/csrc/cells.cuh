@@ -115,6 +115,39 @@ __device__ __forceinline__ void residual_sq(FFAcc &acc, float b, float l, float 
     acc.add(sq, __fadd_rn(sq_err, cross));
 }
 
+// residual_sq for two cells at once (element x: one cell, element y: another),
+// each element with exactly the arithmetic of residual_sq.
+__device__ __forceinline__ void residual_sq2(FFAcc2 &acc, float2 b, float2 l, float2 r, float2 t, float2 bo, float2 c)
+{
+    FF2 s = two_sum2(b, l);
+    float2 e = s.lo;
+    s = two_sum2(s.hi, r);
+    e = __fadd2_rn(e, s.lo);
+    s = two_sum2(s.hi, t);
+    e = __fadd2_rn(e, s.lo);
+    s = two_sum2(s.hi, bo);
+    e = __fadd2_rn(e, s.lo);
+    s = two_sum2(s.hi, __fmul2_rn(make_float2(-4.0f, -4.0f), c));  // -4p is exact
+    e = __fadd2_rn(e, s.lo);
+    const FF2 q = two_sum2(s.hi, e);
+    const float2 sq = __fmul2_rn(q.hi, q.hi);
+    const float2 sq_err = __ffma2_rn(q.hi, q.hi, make_float2(-sq.x, -sq.y));
+    const float2 cross = __fmul2_rn(__fmul2_rn(make_float2(2.0f, 2.0f), q.hi), q.lo);
+    acc.add(sq, __fadd2_rn(sq_err, cross));
+}
+
+// The residual of the four cells a lane holds in row c (float4 x, y, z, w),
+// with the row above `up`, the row below `dn`, the outside neighbours lft
+// (of x) and rgt (of w): cells x, y into acc[0], z, w into acc[1].
+__device__ __forceinline__ void residual_sq4(FFAcc2 (&acc)[2], const float4 &bb, float lft, const float4 &c,
+                                             float rgt, const float4 &up, const float4 &dn)
+{
+    residual_sq2(acc[0], make_float2(bb.x, bb.y), make_float2(lft, c.x), make_float2(c.y, c.z),
+                 make_float2(up.x, up.y), make_float2(dn.x, dn.y), make_float2(c.x, c.y));
+    residual_sq2(acc[1], make_float2(bb.z, bb.w), make_float2(c.y, c.z), make_float2(c.w, rgt),
+                 make_float2(up.z, up.w), make_float2(dn.z, dn.w), make_float2(c.z, c.w));
+}
+
 // Projection, src/fluid.cpp:269-296: u - ((pR-pL)*dt)/2, v - ((pB-pT)*dt)/2
 // (walls: zero on the boundary cells).
 template <int BC = 0>
@@ -156,10 +189,10 @@ __device__ __forceinline__ void project_image_cell(const float *__restrict__ u, 
 }
 
 // Residual sums of one warp task of the strip residual: strip sx (128
-// columns, four per lane), rows [y0, y1). Adds r^2 into acc[0..3] (one chain
-// per lane column) and, with accb, b^2.
+// columns, four per lane), rows [y0, y1). Adds r^2 into acc (one chain per
+// lane column: columns x, y in acc[0], z, w in acc[1]) and, with accb, b^2.
 __device__ __forceinline__ void residual_strip_task(const float *__restrict__ p, const float *__restrict__ b, int ld,
-                                                    int w, int h, int sx, int y0, int y1, int lane, FFAcc (&acc)[4],
+                                                    int w, int h, int sx, int y0, int y1, int lane, FFAcc2 (&acc)[2],
                                                     FFAcc *accb)
 {
     const int x = sx * 128 + 4 * lane;
@@ -181,10 +214,7 @@ __device__ __forceinline__ void residual_strip_task(const float *__restrict__ p,
         if (lane == 0) lft = __ldcg(p + (size_t)y * ld + xl);
         if (lane == last_lane) rgt = __ldcg(p + (size_t)y * ld + xr);
         if (active) {
-            residual_sq(acc[0], bb.x, lft, cu.y, up.x, dn.x, cu.x);
-            residual_sq(acc[1], bb.y, cu.x, cu.z, up.y, dn.y, cu.y);
-            residual_sq(acc[2], bb.z, cu.y, cu.w, up.z, dn.z, cu.z);
-            residual_sq(acc[3], bb.w, cu.z, rgt, up.w, dn.w, cu.w);
+            residual_sq4(acc, bb, lft, cu, rgt, up, dn);
             if (accb) {
                 acc_square(*accb, bb.x);
                 acc_square(*accb, bb.y);

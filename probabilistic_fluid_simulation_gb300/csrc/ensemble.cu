@@ -202,9 +202,9 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             const Member &m = a.mem[mi];
             const int q = t - m.rs_task0, sx = q % m.rsx, sy = q / m.rsx;
             const int y0 = sy * 8, y1 = min(m.h, y0 + 8);
-            FFAcc acc[4];
+            FFAcc2 acc[2];
             residual_strip_task(m.p[(cur + phase) & 1], m.b, m.ld, m.w, m.h, sx, y0, y1, lane, acc, nullptr);
-            const double v = warp_sum((acc[0].value() + acc[1].value()) + (acc[2].value() + acc[3].value()));
+            const double v = warp_sum(acc[0].value() + acc[1].value());
             if (lane == 0) a.rs_part[t] = v;
         }
         if (!grid_sync(a)) return;

@@ -119,6 +119,15 @@ cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, i
                                 const int *done, cudaStream_t st);
 cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
                                 int h, int levels, int halo, int chunk, const int *done, cudaStream_t st);
+// The last launch of a check interval (halo 8, levels 1..7): the fused sweep
+// that also evaluates the exact residual of its output over the grid, as
+// launch_residual does, recording the check in `state` (done at or below tol,
+// with sweeps_here). Needs red.nblocks >= sweep_stream_blocks(w, h, chunk);
+// red.result[1] must hold sum b^2.
+int sweep_stream_blocks(int w, int h, int chunk);
+cudaError_t launch_sweep_stream_check(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
+                                      int h, int levels, int chunk, const Reduce &red, SolveState *state,
+                                      int sweeps_here, double tol, const int *done, cudaStream_t st);
 // 16-bit storage, FP32 compute; pin == null means a zero input iterate. levels in [1, 8].
 cudaError_t launch_sweep_stream_bf16(const __nv_bfloat16 *pin, const __nv_bfloat16 *b, __nv_bfloat16 *pout, int ld,
                                      int w, int h, int levels, int chunk, cudaStream_t st);

@@ -97,5 +97,41 @@ __device__ __forceinline__ void acc_square(FFAcc &acc, float x)
     acc.add(sq, __fmaf_rn(x, x, -sq));
 }
 
+// The same transformations on two independent values at once with the packed
+// f32x2 instructions of sm_100+ (__fadd2_rn, __fmul2_rn, __ffma2_rn round each
+// element to nearest, like their scalar forms), so each element gets exactly
+// the bits of the scalar version in half the issue slots. x - y is
+// fma(y, -1, x): the product is exact, so it is x - y rounded once.
+__device__ __forceinline__ float2 fsub2(float2 x, float2 y) { return __ffma2_rn(y, make_float2(-1.0f, -1.0f), x); }
+
+struct FF2 {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ FF2 two_sum2(float2 a, float2 b)
+{
+    const float2 s = __fadd2_rn(a, b);
+    const float2 bb = fsub2(s, a);
+    const float2 e = __fadd2_rn(fsub2(a, fsub2(s, bb)), fsub2(b, bb));
+    return {s, e};
+}
+
+// Two FFAcc chains (element x and element y) advanced together.
+struct FFAcc2 {
+    float2 hi = make_float2(0.0f, 0.0f), lo = make_float2(0.0f, 0.0f);
+    __device__ __forceinline__ void add(float2 a, float2 a_lo)
+    {
+        const FF2 s = two_sum2(hi, a);
+        const float2 e = __fadd2_rn(s.lo, __fadd2_rn(lo, a_lo));
+        hi = __fadd2_rn(s.hi, e);
+        lo = fsub2(e, fsub2(hi, s.hi));
+    }
+    // (chain x) + (chain y), each converted as FFAcc::value()
+    __device__ __forceinline__ double value() const
+    {
+        return ((double)hi.x + (double)lo.x) + ((double)hi.y + (double)lo.y);
+    }
+};
+
 }  // namespace
 }  // namespace pfs

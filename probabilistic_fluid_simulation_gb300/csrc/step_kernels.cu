@@ -98,14 +98,14 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *
 {
     if (state && *(volatile int *)&state->done) return;  // same answer for every block
     const int lane = threadIdx.x & 31;
-    FFAcc acc[4], accb;  // one accumulator per lane column: four independent chains
+    FFAcc2 acc[2];  // one chain per lane column, two columns per packed accumulator
+    FFAcc accb;
     for (int wid = blockIdx.x * kResWarps + (threadIdx.x >> 5); wid < nwork; wid += gridDim.x * kResWarps) {
         const int sx = wid % nsx, sy = wid / nsx;
         const int y0 = sy * kResChunk, y1 = min(h, y0 + kResChunk);
         residual_strip_task(p, b, ld, w, h, sx, y0, y1, lane, acc, with_b ? &accb : nullptr);
     }
-    reduce_blocks((acc[0].value() + acc[1].value()) + (acc[2].value() + acc[3].value()), red, 0, state, sweeps_here,
-                  tol);
+    reduce_blocks(acc[0].value() + acc[1].value(), red, 0, state, sweeps_here, tol);
     if (with_b) {
         __syncthreads();
         reduce_blocks(accb.value(), red, 1);

@@ -3,8 +3,10 @@
 // (ensemble.cu). See sweep_kernels.cu for the design.
 #pragma once
 
+#include "cells.cuh"
 #include "common.cuh"
 #include "kernels.h"
+#include "reduce.cuh"
 #include "storage.cuh"
 
 namespace pfs {
@@ -45,6 +47,11 @@ struct StreamArgs {
     const int *done;  // solve already converged: return at once
     int ld, w, h;
     int nsx, nwork, chunk;
+    // launches that also evaluate the residual of their last level (a check point)
+    Reduce red;          // partials for one block per 4 warp tasks; result[1] holds sum b^2
+    SolveState *state;   // records the check, raises done at or below tol
+    int sweeps_here;     // sweep count of the solve after this launch
+    double tol;
 };
 
 // Rows in flight per warp (cp.async prefetch depth).
@@ -54,13 +61,14 @@ constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
 
 // Register rings of the pipeline. Level s (0..L-1) keeps rows y-s-2, y-s-1,
 // y-s in three register sets whose roles rotate with period 3; the divergence
-// rows y-1 .. y-L plus the row being loaded live in a ring of L+1 registers.
-// Unrolling the row loop by U = lcm(3, L+1) makes every ring index a
-// compile-time register name: no register moves, one shared-memory read of b
-// per row instead of one per level.
-template <typename T, int L>
+// rows y-1 .. y-L plus the row being loaded live in a ring of L+1 registers
+// (L+2 when the launch also evaluates the residual of level L, which needs b
+// one row further back). Unrolling the row loop by U = lcm(3, NB) makes every
+// ring index a compile-time register name: no register moves, one
+// shared-memory read of b per row instead of one per level.
+template <typename T, int L, bool RES = false>
 struct Ring {
-    static constexpr int NB = L + 1;
+    static constexpr int NB = L + 1 + (RES ? 1 : 0);
     static constexpr int U = 3 * NB / gcd_c(3, NB);
     static constexpr int vecs_per_warp = 2 * kRP * 32;  // p and b prefetch rings, one vector per lane and row
     static constexpr int bytes_per_block = 4 * vecs_per_warp * Store<T>::vec_bytes;
@@ -112,13 +120,18 @@ __device__ __forceinline__ void prefetch_row(Cursor<T> &cu, typename Store<T>::V
 
 // One row step t of the pipeline (load row y = ybeg + t); K = t mod U is a
 // compile-time constant, so R[K % 3]... and bq[...] name fixed registers.
-template <typename T, int L, bool PREV, int K>
-__device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[L + 1],
-                                            typename Store<T>::Vec *pr, typename Store<T>::Vec *br, Cursor<T> &cu,
-                                            const StreamArgs<T> &a, int nsteps, int rows, T *out, T *outp)
+// With RES, TR keeps the last three level-L rows (period 3) and the step adds
+// the exact squared residual of level L at row y-L-1 (the row stored at the
+// previous step) into acc, with the per-cell arithmetic of the residual
+// kernels (residual_sq), for the stored lanes only.
+template <typename T, int L, bool PREV, bool RES, int K>
+__device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB],
+                                            float4 (&TR)[3], FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
+                                            typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
+                                            int nsteps, int rows, T *out, T *outp)
 {
     using V = typename Store<T>::Vec;
-    constexpr int NB = L + 1;
+    constexpr int NB = Ring<T, L, RES>::NB;
     float4(&P)[L] = R[K % 3];
     float4(&Cur)[L] = R[(K + 1) % 3];
     float4(&N)[L] = R[(K + 2) % 3];
@@ -138,19 +151,31 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
     if (out && (unsigned)cu.st_rel < (unsigned)rows) *reinterpret_cast<V *>(out + cu.st_off) = Store<T>::from_f4(top);
     if (PREV && outp && (unsigned)(cu.st_rel + 1) < (unsigned)rows)
         *reinterpret_cast<V *>(outp + cu.st_off + a.ld) = Store<T>::from_f4(N[L - 1]);
+    if constexpr (RES) {
+        TR[K % 3] = top;                                  // level L, row y-L
+        const float4 &c = TR[(K + 2) % 3];                // row y-L-1
+        const float4 &up = TR[(K + 1) % 3];               // row y-L-2
+        const float4 &bb = bq[(K + NB * (L + 1) - L - 1) % NB];  // b of row y-L-1
+        const float lft = __shfl_up_sync(0xffffffffu, c.w, 1);
+        const float rgt = __shfl_down_sync(0xffffffffu, c.x, 1);
+        if (out && (unsigned)(cu.st_rel - 1) < (unsigned)rows) {
+            residual_sq4(acc, bb, lft, c, rgt, up, top);
+        }
+    }
     cu.st_off += a.ld;
     cu.st_rel += 1;
 }
 
-template <typename T, int L, bool PREV, int K>
-__device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[L + 1],
-                                             typename Store<T>::Vec *pr, typename Store<T>::Vec *br, Cursor<T> &cu,
-                                             const StreamArgs<T> &a, int nsteps, int rows, T *out, T *outp)
+template <typename T, int L, bool PREV, bool RES, int K>
+__device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB],
+                                             float4 (&TR)[3], FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
+                                             typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
+                                             int nsteps, int rows, T *out, T *outp)
 {
-    if constexpr (K < Ring<T, L>::U) {
+    if constexpr (K < Ring<T, L, RES>::U) {
         if (t + K < nsteps) {
-            stream_step<T, L, PREV, K>(t + K, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
-            stream_steps<T, L, PREV, K + 1>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_step<T, L, PREV, RES, K>(t + K, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_steps<T, L, PREV, RES, K + 1>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
         }
     }
 }
@@ -162,10 +187,16 @@ constexpr int min_blocks() { return L >= 7 ? 2 : 3; }
 
 // One warp task of the fused sweep: strip wid % nsx, row chunk wid / nsx.
 // `ring` is this warp's shared-memory ring (Ring<T, L>::vecs_per_warp vectors).
-template <typename T, int G, int L, bool PREV>
-__device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int lane, typename Store<T>::Vec *ring)
+// With RES the task also adds the squared residual of level L over its stored
+// cells into acc: it loads one more halo row at each end (level L is then
+// valid one row beyond the chunk), and L < G keeps level L valid one column
+// beyond the stored lanes.
+template <typename T, int G, int L, bool PREV, bool RES = false>
+__device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int lane, typename Store<T>::Vec *ring,
+                                            FFAcc2 (&acc)[2])
 {
     static_assert(L >= 1 && L <= G && G % 4 == 0, "fusion depth must fit the halo");
+    static_assert(!RES || L < G, "the residual needs level L one column beyond the stored lanes");
     using V = typename Store<T>::Vec;
     const int sx = wid % a.nsx, sy = wid / a.nsx;
     const int xo = sx * (128 - 2 * G);
@@ -175,8 +206,9 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     const bool st_lane = lane >= G / 4 && lane < 32 - G / 4 && xl < a.w;
     const int y0 = sy * a.chunk;
     const int rows = min(a.h, y0 + a.chunk) - y0;
-    const int ybeg = y0 - L;
-    const int nsteps = rows + 2 * L;
+    constexpr int E = RES ? L + 1 : L;  // halo rows loaded at each end
+    const int ybeg = y0 - E;
+    const int nsteps = rows + 2 * E;
 
     V *pr = ring + lane;
     V *br = pr + kRP * 32;
@@ -186,8 +218,8 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     if (cu.ld_row < 0) cu.ld_row += a.h;
     cu.gp = a.pin + (size_t)cu.ld_row * a.ld + cx;
     cu.gb = a.b + (size_t)cu.ld_row * a.ld + cx;
-    cu.st_rel = -2 * L;  // level L at step 0 is row ybeg - L = y0 - 2L
-    cu.st_off = (long long)(y0 - 2 * L) * a.ld;
+    cu.st_rel = -E - L;  // level L at step 0 is row ybeg - L = y0 - E - L
+    cu.st_off = (long long)(y0 - E - L) * a.ld;
     T *out = st_lane ? a.pout + cx : nullptr;
     T *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
 #pragma unroll
@@ -196,16 +228,25 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
         cp_async_commit();
     }
 
-    float4 R[3][L], bq[L + 1];
+    constexpr int NB = Ring<T, L, RES>::NB;
+    float4 R[3][L], bq[NB], TR[3];
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int s = 0; s < L; ++s) R[0][s] = R[1][s] = R[2][s] = z;
 #pragma unroll
-    for (int s = 0; s <= L; ++s) bq[s] = z;
+    for (int s = 0; s < NB; ++s) bq[s] = z;
+    TR[0] = TR[1] = TR[2] = z;
 
-    for (int t = 0; t < nsteps; t += Ring<T, L>::U)
-        stream_steps<T, L, PREV, 0>(t, R, bq, pr, br, cu, a, nsteps, rows, out, outp);
+    for (int t = 0; t < nsteps; t += Ring<T, L, RES>::U)
+        stream_steps<T, L, PREV, RES, 0>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
     cp_async_wait<0>();
+}
+
+template <typename T, int G, int L, bool PREV>
+__device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int lane, typename Store<T>::Vec *ring)
+{
+    FFAcc2 unused[2];
+    stream_task<T, G, L, PREV, false>(a, wid, lane, ring, unused);
 }
 
 }  // namespace

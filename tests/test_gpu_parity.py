@@ -304,3 +304,59 @@ def test_dropin_rejects_bad_input_on_gpu(cuda_device, pfs_lib):
     img = torch.zeros(8, 8, 3, device="cuda")
     with pytest.raises(pfs_lib.PFSError):
         pfs_lib.advect_color_step(img, img, vp, 0.1)
+
+
+# The last fused launch of each check interval evaluates the residual itself
+# (launch_sweep_stream_check); grids whose check launch would exceed the
+# reduction's capacity (chunks under 16 rows) take the separate residual kernel.
+# Both must give the oracle's sweeps, residuals and bits.
+@pytest.mark.parametrize("every", [64, 100, 24])
+def test_fused_check_matches_separate_residual_and_oracle(cuda_device, pfs_lib, oracle_mod, every):
+    w, h = 256, 192
+    vp, tmp, img, itmp = S.initial_state(w, h, 3, seed=31)
+    tol, cap = 3e-3, 6000  # converges in 3984-4700 sweeps per step
+    ov, ot, oi, ost = oracle_run(oracle_mod, vp.copy(), tmp.copy(), img.copy(), itmp.copy(), 2, 0.1, 0.0, 40,
+                                 cap, tol=tol, check_every=every)
+    runs = []
+    for chunk in (32, 8):  # fused check / separate residual kernel
+        with pfs_lib.Session(w, h, image_shape=img.shape, dt=0.1, diffuse_iters=40, max_iters=cap, tol=tol,
+                             check_every=every, chunk_rows=chunk) as s:
+            s.upload(vp, tmp, img)
+            stats = []
+            for _ in range(2):
+                s.step(1)
+                stats.append(s.stats())
+            a, b, c = np.empty_like(vp), np.empty_like(tmp), np.empty_like(img)
+            s.download(a, b, c)
+        runs.append((stats, a, b, c))
+    for stats, a, b, c in runs:
+        assert [x["sweeps"] for x in stats] == [x.sweeps for x in ost]
+        assert [x["checks"] for x in stats] == [x.sweeps // every + (x.sweeps % every != 0) for x in ost]
+        for x, o in zip(stats, ost):
+            assert x["rel_residual"] == pytest.approx(o.rel_residual, rel=1e-9)
+        assert_same(a, ov, "vp")
+        assert_same(b, ot, "tmp")
+        assert_same(c, oi, "image")
+    assert all(x.sweeps < cap for x in ost)
+
+
+def test_fused_check_on_a_large_grid(cuda_device, pfs_lib):
+    """4096x4096: the check launch has 1184 blocks, more than the 608 of the
+    separate residual kernel; checks every 16 sweeps, cap 48. The fused check
+    and the separate kernel (chunk 8) give the same bits and residuals."""
+    w = h = 4096
+    vp, tmp, img, _ = S.initial_state(w, h, 3, seed=2)
+    out = []
+    for chunk in (32, 8):
+        with pfs_lib.Session(w, h, dt=0.05, diffuse_iters=2, max_iters=48, tol=1e-12, check_every=16,
+                             chunk_rows=chunk) as s:
+            s.upload(vp, tmp)
+            s.step(1)
+            st = s.stats()
+            a = np.empty_like(vp)
+            s.download(a)
+        out.append((st, a))
+    (s1, a1), (s2, a2) = out
+    assert s1["sweeps"] == s2["sweeps"] == 48 and s1["checks"] == s2["checks"] == 3 and s1["capped"]
+    assert s1["rel_residual"] == pytest.approx(s2["rel_residual"], rel=1e-12)
+    assert np.array_equal(a1, a2)
