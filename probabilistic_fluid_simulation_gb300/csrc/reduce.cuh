@@ -36,8 +36,20 @@ __device__ void reduce_blocks(double acc, const Reduce &red, int slot, SolveStat
     __syncthreads();
     if (last && wid == 0) {
         __threadfence();
+        // lane sums partials lane, lane + 32, ... in that order; the loads are
+        // issued eight at a time so the tail does not wait on one L2 round trip
+        // per partial (the same additions in the same order as a plain loop)
         double s = 0.0;
-        for (int k = lane; k < (int)gridDim.x; k += 32) s += __ldcg(red.partials + k * 2 + slot);
+        const int n = (int)gridDim.x;
+        int k = lane;
+        for (; k + 32 * 7 < n; k += 32 * 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = __ldcg(red.partials + (k + 32 * u) * 2 + slot);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += v[u];
+        }
+        for (; k < n; k += 32) s += __ldcg(red.partials + k * 2 + slot);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0) {

@@ -305,12 +305,12 @@ cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
     return launched();
 }
 
-// A few words copied (src non-null) or zeroed by one warp; stores to mapped
-// host memory are made visible to the host before the kernel completes.
+// A few words copied (src non-null) or zeroed by one warp. Stores to mapped
+// host memory are visible to the host once it has seen the kernel complete
+// (a stream or event synchronisation).
 __global__ void k_small_words(const unsigned *__restrict__ src, unsigned *__restrict__ dst, int words)
 {
     for (int k = threadIdx.x; k < words; k += 32) dst[k] = src ? src[k] : 0u;
-    __threadfence_system();
 }
 
 cudaError_t launch_copy_small(const void *src, void *dst, size_t bytes, cudaStream_t st)

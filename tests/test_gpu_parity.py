@@ -307,9 +307,10 @@ def test_dropin_rejects_bad_input_on_gpu(cuda_device, pfs_lib):
 
 
 # The last fused launch of each check interval evaluates the residual itself
-# (launch_sweep_stream_check); grids whose check launch would exceed the
-# reduction's capacity (chunks under 16 rows) take the separate residual kernel.
-# Both must give the oracle's sweeps, residuals and bits.
+# (launch_sweep_stream_check). Check intervals that are multiples of 8 split
+# their last 8-level launch in two (64); chunks of 32 and 8 rows give the check
+# launch different geometries. Each must give the oracle's sweeps, residuals
+# and bits.
 @pytest.mark.parametrize("every", [64, 100, 24])
 def test_fused_check_matches_separate_residual_and_oracle(cuda_device, pfs_lib, oracle_mod, every):
     w, h = 256, 192
@@ -318,7 +319,7 @@ def test_fused_check_matches_separate_residual_and_oracle(cuda_device, pfs_lib, 
     ov, ot, oi, ost = oracle_run(oracle_mod, vp.copy(), tmp.copy(), img.copy(), itmp.copy(), 2, 0.1, 0.0, 40,
                                  cap, tol=tol, check_every=every)
     runs = []
-    for chunk in (32, 8):  # fused check / separate residual kernel
+    for chunk in (32, 8):
         with pfs_lib.Session(w, h, image_shape=img.shape, dt=0.1, diffuse_iters=40, max_iters=cap, tol=tol,
                              check_every=every, chunk_rows=chunk) as s:
             s.upload(vp, tmp, img)
@@ -341,9 +342,11 @@ def test_fused_check_matches_separate_residual_and_oracle(cuda_device, pfs_lib, 
 
 
 def test_fused_check_on_a_large_grid(cuda_device, pfs_lib):
-    """4096x4096: the check launch has 1184 blocks, more than the 608 of the
-    separate residual kernel; checks every 16 sweeps, cap 48. The fused check
-    and the separate kernel (chunk 8) give the same bits and residuals."""
+    """4096x4096, checks every 16 sweeps, cap 48: with 32-row chunks the check
+    launch has 1184 blocks (more than the 608 of the separate residual
+    kernel); with 8-row chunks it would need more partials than the field
+    holds, so the separate residual kernel runs. Both give the same bits and
+    residuals."""
     w = h = 4096
     vp, tmp, img, _ = S.initial_state(w, h, 3, seed=2)
     out = []
