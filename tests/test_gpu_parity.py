@@ -363,3 +363,27 @@ def test_fused_check_on_a_large_grid(cuda_device, pfs_lib):
     assert s1["sweeps"] == s2["sweeps"] == 48 and s1["checks"] == s2["checks"] == 3 and s1["capped"]
     assert s1["rel_residual"] == pytest.approx(s2["rel_residual"], rel=1e-12)
     assert np.array_equal(a1, a2)
+
+
+@pytest.mark.parametrize("w,h", [(8, 2), (4, 3), (12, 1), (16, 5)])
+@pytest.mark.parametrize("every", [3, 8])
+def test_fused_check_tiny_grids(cuda_device, pfs_lib, oracle_mod, w, h, every):
+    """Grids of 1-5 rows: the check launch's extra halo rows wrap around the
+    grid several times; intervals of 3 (3-level check launches) and 8 (split
+    4 + 4). Sweeps, residuals and every buffer as the oracle."""
+    vp, tmp, _, _ = S.initial_state(w, h, 3, seed=5)
+    ov, ot, _, ost = oracle_run(oracle_mod, vp.copy(), tmp.copy(), None, None, 2, 0.1, 0.0, 4, 200, tol=1e-3,
+                                check_every=every)
+    with pfs_lib.Session(w, h, dt=0.1, diffuse_iters=4, max_iters=200, tol=1e-3, check_every=every) as s:
+        s.upload(vp, tmp)
+        stats = []
+        for _ in range(2):
+            s.step(1)
+            stats.append(s.stats())
+        a, b = np.empty_like(vp), np.empty_like(tmp)
+        s.download(a, b)
+    assert [x["sweeps"] for x in stats] == [x.sweeps for x in ost]
+    for x, o in zip(stats, ost):
+        assert x["rel_residual"] == pytest.approx(o.rel_residual, rel=1e-9)
+    assert_same(a, ov, "vp")
+    assert_same(b, ot, "tmp")
