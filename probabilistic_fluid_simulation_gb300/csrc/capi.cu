@@ -970,15 +970,16 @@ int pfs_session_upload(pfs_session *s, const float *vp, const float *tmp, const 
 // made on first use.
 static int io_init(pfs_session *s)
 {
-    if (s->up_st) return PFS_OK;
+    if (s->up_st) return PFS_OK;  // made last: everything else is in place
     const size_t vcount = (size_t)s->f.w * s->f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
     s->io_floats = 2 * vcount + icount;
+    // each piece only if missing, so a call after a failed one completes the set without leaking
     for (pfs_session::IoSlot *k : {&s->up[0], &s->up[1], &s->down[0], &s->down[1]}) {
-        CK(cudaMalloc(&k->buf, s->io_floats * sizeof(float)));
-        CK(cudaEventCreateWithFlags(&k->copied, cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&k->used, cudaEventDisableTiming));
+        if (!k->buf) CK(cudaMalloc(&k->buf, s->io_floats * sizeof(float)));
+        if (!k->copied) CK(cudaEventCreateWithFlags(&k->copied, cudaEventDisableTiming));
+        if (!k->used) CK(cudaEventCreateWithFlags(&k->used, cudaEventDisableTiming));
     }
-    CK(cudaStreamCreateWithFlags(&s->down_st, cudaStreamNonBlocking));
+    if (!s->down_st) CK(cudaStreamCreateWithFlags(&s->down_st, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&s->up_st, cudaStreamNonBlocking));
     return PFS_OK;
 }
