@@ -100,6 +100,9 @@ struct Field {
     // red's result and tickets
     double *psweep = nullptr;
     Reduce red_sweep{};
+    // check intervals in the first batch of the next residual-mode solve: 1 after a solve that
+    // converged (doubling from there), 16 after one that ran to the cap without converging
+    int first_batch = 1;
     // residual checks run here, overlapping the sweep launch that follows them
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_check = nullptr, ev_res = nullptr;
@@ -277,7 +280,7 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     };
 
     CheckPoint marks[64];
-    int nmarks = 0, batch = 1, in_batch = 0;
+    int nmarks = 0, batch = f.first_batch, in_batch = 0;
     int S = 0;
     bool finished = false;
     // predicted start: watch every check; if the residual does not fall, restart from the plain start
@@ -364,6 +367,10 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     }
     o.sweeps = S;
     o.capped = resid && S == c.S && !(o.rel <= c.tol);
+    // a solve that ran to the cap is likely followed by another: enqueue its checks in one batch of
+    // 16 (one host read of the state instead of five for 20 checks); any converged solve resets to
+    // doubling from 1, so at most one step after a change enqueues intervals that return at once
+    if (resid) f.first_batch = o.capped ? 16 : 1;
     if (c.want_res && !resid) {
         double rr, bb;
         CKS(residual_host(f, f.p[cur], st, rr, bb));

@@ -387,3 +387,36 @@ def test_fused_check_tiny_grids(cuda_device, pfs_lib, oracle_mod, w, h, every):
         assert x["rel_residual"] == pytest.approx(o.rel_residual, rel=1e-9)
     assert_same(a, ov, "vp")
     assert_same(b, ot, "tmp")
+
+
+def test_capped_step_then_converging_step(cuda_device, pfs_lib, oracle_mod):
+    """After a step that runs to the cap the next solve enqueues 16 check
+    intervals before reading the state; when that step converges early the
+    intervals after the converged check return at once, and the step still
+    ends at the oracle's sweep count with its buffers."""
+    w, h = 64, 48
+    vp, tmp, img, itmp = S.initial_state(w, h, 3, seed=21)
+    tol, every = 1e-4, 100  # then 900 and 1100 sweeps: converged inside the first 16 intervals
+    v1, t1, i1, s1 = oracle_run(oracle_mod, vp.copy(), tmp.copy(), img.copy(), itmp.copy(), 1, 0.1, 0.0, 40, 300,
+                                tol=tol, check_every=every)
+    v2, t2, i2, s2 = oracle_run(oracle_mod, v1, t1, i1, np.zeros_like(img), 2, 0.1, 0.0, 40, 3000, tol=tol,
+                                check_every=every)
+    assert s1[0].sweeps == 300 and all(x.sweeps < 3000 and x.sweeps // every < 16 for x in s2)
+    with pfs_lib.Session(w, h, image_shape=img.shape, dt=0.1, diffuse_iters=40, max_iters=300, tol=tol,
+                         check_every=every) as s:
+        s.upload(vp, tmp, img)
+        s.step(1)
+        assert s.stats()["capped"] == 1
+        s.set_params(max_iters=3000)
+        got = []
+        for _ in range(2):
+            s.step(1)
+            got.append(s.stats())
+        a, b, c = np.empty_like(vp), np.empty_like(tmp), np.empty_like(img)
+        s.download(a, b, c)
+    assert [x["sweeps"] for x in got] == [x.sweeps for x in s2]
+    for x, o in zip(got, s2):
+        assert x["rel_residual"] == pytest.approx(o.rel_residual, rel=1e-9) and not x["capped"]
+    assert_same(a, v2, "vp")
+    assert_same(b, t2, "tmp")
+    assert_same(c, i2, "image")
