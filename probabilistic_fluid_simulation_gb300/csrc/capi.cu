@@ -101,7 +101,8 @@ struct Field {
     double *psweep = nullptr;
     Reduce red_sweep{};
     // check intervals in the first batch of the next residual-mode solve: 1 after a solve that
-    // converged (doubling from there), 16 after one that ran to the cap without converging
+    // converged (doubling from there), as many as the capped one checked (at most 64) after one
+    // that ran to the cap without converging
     int first_batch = 1;
     // residual checks run here, overlapping the sweep launch that follows them
     cudaStream_t aux = nullptr;
@@ -243,8 +244,9 @@ struct CheckPoint {
 // relative residual on the device and raises SolveState::done once it is at
 // or below tol, which turns every later sweep and residual launch of the
 // solve into an immediate return. The host enqueues check intervals in
-// batches that double in size (1, 2, 4, ...) and reads the state only between
-// batches, then takes the plane roles recorded at the converged check point.
+// batches that double in size (1, 2, 4, ...; after a capped solve the first
+// batch covers all its checks) and reads the state only between batches, then
+// takes the plane roles recorded at the converged check point.
 //
 // With the fused sweep (width a multiple of 4) the last launch of each check
 // interval evaluates the exact residual of its output itself
@@ -367,10 +369,10 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
     }
     o.sweeps = S;
     o.capped = resid && S == c.S && !(o.rel <= c.tol);
-    // a solve that ran to the cap is likely followed by another: enqueue its checks in one batch of
-    // 16 (one host read of the state instead of five for 20 checks); any converged solve resets to
+    // a solve that ran to the cap is likely followed by another: enqueue all its checks in one batch
+    // (one host read of the state instead of five for 20 checks); any converged solve resets to
     // doubling from 1, so at most one step after a change enqueues intervals that return at once
-    if (resid) f.first_batch = o.capped ? 16 : 1;
+    if (resid) f.first_batch = o.capped ? std::max(1, std::min(64, o.checks)) : 1;
     if (c.want_res && !resid) {
         double rr, bb;
         CKS(residual_host(f, f.p[cur], st, rr, bb));

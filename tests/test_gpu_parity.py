@@ -390,19 +390,20 @@ def test_fused_check_tiny_grids(cuda_device, pfs_lib, oracle_mod, w, h, every):
 
 
 def test_capped_step_then_converging_step(cuda_device, pfs_lib, oracle_mod):
-    """After a step that runs to the cap the next solve enqueues 16 check
-    intervals before reading the state; when that step converges early the
-    intervals after the converged check return at once, and the step still
-    ends at the oracle's sweep count with its buffers."""
+    """After a step that runs to the cap (8 checks) the next solve enqueues 8
+    check intervals before reading the state, then 16 more; it converges at
+    the 10th, the 14 intervals after it return at once, and the step still
+    ends at the oracle's sweep count with its buffers; the step after a
+    converged one starts from a batch of 1 again."""
     w, h = 64, 48
     vp, tmp, img, itmp = S.initial_state(w, h, 3, seed=21)
-    tol, every = 1e-4, 100  # then 900 and 1100 sweeps: converged inside the first 16 intervals
-    v1, t1, i1, s1 = oracle_run(oracle_mod, vp.copy(), tmp.copy(), img.copy(), itmp.copy(), 1, 0.1, 0.0, 40, 300,
+    tol, every = 1e-4, 100
+    v1, t1, i1, s1 = oracle_run(oracle_mod, vp.copy(), tmp.copy(), img.copy(), itmp.copy(), 1, 0.1, 0.0, 40, 800,
                                 tol=tol, check_every=every)
     v2, t2, i2, s2 = oracle_run(oracle_mod, v1, t1, i1, np.zeros_like(img), 2, 0.1, 0.0, 40, 3000, tol=tol,
                                 check_every=every)
-    assert s1[0].sweeps == 300 and all(x.sweeps < 3000 and x.sweeps // every < 16 for x in s2)
-    with pfs_lib.Session(w, h, image_shape=img.shape, dt=0.1, diffuse_iters=40, max_iters=300, tol=tol,
+    assert s1[0].sweeps == 800 and all(800 < x.sweeps < 3000 for x in s2)
+    with pfs_lib.Session(w, h, image_shape=img.shape, dt=0.1, diffuse_iters=40, max_iters=800, tol=tol,
                          check_every=every) as s:
         s.upload(vp, tmp, img)
         s.step(1)
