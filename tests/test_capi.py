@@ -79,3 +79,17 @@ def test_host_call_shape_checks(pfs_lib):
 def test_params_default(pfs_lib):
     p = pfs_lib.default_params()
     assert p.dt == pytest.approx(0.1) and p.max_iters == 30 and p.diffuse_iters == 30 and p.tol == 0.0
+
+
+def test_headers_compile_as_c_and_cxx():
+    """include/pfs.h is plain C (a cgo / JNI / FFI binding includes it as
+    such) and also valid C++."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc") or not shutil.which("g++"):
+        pytest.skip("no host compiler")
+    hdr = os.path.join(ROOT, "include", "pfs.h")
+    for cmd in (["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c", hdr],
+                ["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c++", hdr]):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
