@@ -12,25 +12,25 @@ namespace png {
 namespace {
 
 // ---------------------------------------------------------------- checksums
-uint32_t crc_table[256];
-bool crc_ready = false;
-
-void crc_init()
-{
-    if (crc_ready) return;
-    for (uint32_t n = 0; n < 256; ++n) {
-        uint32_t c = n;
-        for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-        crc_table[n] = c;
+// The table is built once, when first needed, by a function-local static
+// (initialisation is thread-safe: frames are encoded on several threads).
+struct CrcTable {
+    uint32_t t[256];
+    CrcTable()
+    {
+        for (uint32_t n = 0; n < 256; ++n) {
+            uint32_t c = n;
+            for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            t[n] = c;
+        }
     }
-    crc_ready = true;
-}
+};
 
 uint32_t crc32(const uint8_t *p, size_t n, uint32_t c = 0)
 {
-    crc_init();
+    static const CrcTable table;
     c ^= 0xFFFFFFFFu;
-    for (size_t i = 0; i < n; ++i) c = crc_table[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
+    for (size_t i = 0; i < n; ++i) c = table.t[(c ^ p[i]) & 0xFFu] ^ (c >> 8);
     return c ^ 0xFFFFFFFFu;
 }
 
@@ -241,58 +241,119 @@ bool inflate_raw(BitIn &b, std::vector<uint8_t> &out, std::string &err)
 }
 
 // ---------------------------------------------------------------- deflate (fixed codes)
+// Bits go out least significant first through a 64-bit accumulator; Huffman
+// codes are stored bit-reversed in tables, so every symbol is one put.
 struct BitOut {
     std::vector<uint8_t> &v;
-    uint32_t buf = 0;
+    uint64_t buf = 0;
     int cnt = 0;
     explicit BitOut(std::vector<uint8_t> &out) : v(out) {}
-    void put(uint32_t value, int n)  // LSB first
+    void put(uint32_t value, int n)  // n <= 32
     {
-        buf |= value << cnt;
+        buf |= (uint64_t)value << cnt;
         cnt += n;
-        while (cnt >= 8) {
+        if (cnt >= 32) {
+            for (int k = 0; k < 4; ++k) v.push_back((uint8_t)(buf >> (8 * k)));
+            buf >>= 32;
+            cnt -= 32;
+        }
+    }
+    void flush()
+    {
+        while (cnt > 0) {
             v.push_back((uint8_t)buf);
             buf >>= 8;
             cnt -= 8;
         }
-    }
-    void put_code(uint32_t code, int n)  // Huffman codes go most significant bit first
-    {
-        uint32_t r = 0;
-        for (int k = 0; k < n; ++k) r |= ((code >> k) & 1u) << (n - 1 - k);
-        put(r, n);
-    }
-    void flush()
-    {
-        if (cnt > 0) v.push_back((uint8_t)buf);
         buf = 0;
         cnt = 0;
     }
 };
 
-void put_literal(BitOut &o, int s)
+uint32_t reverse_bits(uint32_t code, int n)
 {
-    if (s < 144) o.put_code(0x30 + s, 8);
-    else if (s < 256) o.put_code(0x190 + (s - 144), 9);
-    else if (s < 280) o.put_code(s - 256, 7);
-    else o.put_code(0xC0 + (s - 280), 8);
+    uint32_t r = 0;
+    for (int k = 0; k < n; ++k) r |= ((code >> k) & 1u) << (n - 1 - k);
+    return r;
 }
 
-void put_match(BitOut &o, int len, int dist)
+// The fixed literal/length code (RFC 1951 3.2.6), bit-reversed, and for every
+// match length 3..258 its code (with the extra bits merged in) and total bit
+// count; for distances 1..32768 the same through zlib-style two-level indexing.
+struct FixedCodes {
+    uint32_t lit[288];
+    uint8_t lit_bits[288];
+    uint32_t len_code[259];
+    uint8_t len_bits[259];
+    uint8_t dist_sym[512];
+    uint32_t dist_rev[30];  // the 5-bit distance codes, bit-reversed
+    FixedCodes()
+    {
+        for (int j = 0; j < 30; ++j) dist_rev[j] = reverse_bits((uint32_t)j, 5);
+        for (int s = 0; s < 288; ++s) {
+            uint32_t c;
+            int n;
+            if (s < 144) c = 0x30 + s, n = 8;
+            else if (s < 256) c = 0x190 + (s - 144), n = 9;
+            else if (s < 280) c = s - 256, n = 7;
+            else c = 0xC0 + (s - 280), n = 8;
+            lit[s] = reverse_bits(c, n);
+            lit_bits[s] = (uint8_t)n;
+        }
+        for (int len = 3; len <= 258; ++len) {
+            int k = 28;
+            while (kLenBase[k] > len) --k;
+            const int sym = 257 + k;
+            len_code[len] = lit[sym] | ((uint32_t)(len - kLenBase[k]) << lit_bits[sym]);
+            len_bits[len] = (uint8_t)(lit_bits[sym] + kLenExtra[k]);
+        }
+        for (int d = 1; d <= 32768; ++d) {
+            int j = 29;
+            while (kDistBase[j] > d) --j;
+            if (d <= 256) dist_sym[d - 1] = (uint8_t)j;
+            else dist_sym[256 + ((d - 1) >> 7)] = (uint8_t)j;
+        }
+    }
+    int dsym(int d) const { return d <= 256 ? dist_sym[d - 1] : dist_sym[256 + ((d - 1) >> 7)]; }
+};
+
+const FixedCodes &fixed_codes()
 {
-    int k = 28;
-    while (kLenBase[k] > len) --k;
-    put_literal(o, 257 + k);
-    if (kLenExtra[k]) o.put(len - kLenBase[k], kLenExtra[k]);
-    int j = 29;
-    while (kDistBase[j] > dist) --j;
-    o.put_code(j, 5);
-    if (kDistExtra[j]) o.put(dist - kDistBase[j], kDistExtra[j]);
+    static const FixedCodes c;  // thread-safe one-time initialisation
+    return c;
 }
 
+// Length of the common prefix of a and b, at most maxlen, 8 bytes at a time.
+inline size_t match_len(const uint8_t *a, const uint8_t *b, size_t maxlen)
+{
+    size_t l = 0;
+    while (l + 8 <= maxlen) {
+        uint64_t x, y;
+        std::memcpy(&x, a + l, 8);
+        std::memcpy(&y, b + l, 8);
+        const uint64_t z = x ^ y;
+        if (z) {
+            // first differing byte: the lowest set byte of z on a little-endian host, the highest otherwise
+            const uint16_t probe = 1;
+            const bool le = *reinterpret_cast<const uint8_t *>(&probe) == 1;
+            return l + (size_t)((le ? __builtin_ctzll(z) : __builtin_clzll(z)) >> 3);
+        }
+        l += 8;
+    }
+    while (l < maxlen && a[l] == b[l]) ++l;
+    return l;
+}
+
+// One final block with the fixed codes. Matches come from hash chains over a
+// 32 KiB window (3-byte hash): up to kMaxChain candidates per position, the
+// search stopping at a match of kNiceLen bytes; every position of a match of
+// up to kMaxInsert bytes enters the chains, longer matches insert their first
+// and last kMaxInsert positions (long runs repeat themselves, and inserting
+// every byte of them made the encoder three times slower).
 void deflate_fixed(const uint8_t *d, size_t n, std::vector<uint8_t> &out)
 {
-    constexpr int kWin = 32768, kHashBits = 15, kMaxChain = 32, kMaxLen = 258;
+    constexpr int kWin = 32768, kHashBits = 15, kMaxChain = 16, kMaxLen = 258, kNiceLen = 128, kMaxInsert = 16;
+    const FixedCodes &fc = fixed_codes();
     std::vector<int> head(1 << kHashBits, -1), prev(kWin, -1);
     auto hash = [&](size_t i) {
         return (int)((((uint32_t)d[i] << 16) ^ ((uint32_t)d[i + 1] << 8) ^ d[i + 2]) * 2654435761u >> (32 - kHashBits));
@@ -303,6 +364,7 @@ void deflate_fixed(const uint8_t *d, size_t n, std::vector<uint8_t> &out)
         prev[i & (kWin - 1)] = head[h];
         head[h] = (int)i;
     };
+    out.reserve(out.size() + n / 4 + 64);
     BitOut o(out);
     o.put(1, 1);  // final block
     o.put(1, 2);  // fixed Huffman codes
@@ -315,12 +377,13 @@ void deflate_fixed(const uint8_t *d, size_t n, std::vector<uint8_t> &out)
             for (int chain = 0; cand >= 0 && chain < kMaxChain; ++chain) {
                 const size_t dist = i - (size_t)cand;
                 if (dist == 0 || dist > (size_t)kWin - 1) break;
-                size_t l = 0;
-                while (l < maxlen && d[cand + l] == d[i + l]) ++l;
-                if ((int)l > best) {
-                    best = (int)l;
-                    bestd = (int)dist;
-                    if (l == maxlen) break;
+                if (d[cand + best] == d[i + best]) {  // can this candidate beat the best so far?
+                    const size_t l = match_len(d + cand, d + i, maxlen);
+                    if ((int)l > best) {
+                        best = (int)l;
+                        bestd = (int)dist;
+                        if (l >= (size_t)kNiceLen || l == maxlen) break;
+                    }
                 }
                 const int nxt = prev[cand & (kWin - 1)];
                 if (nxt >= cand) break;  // the window slot was reused
@@ -328,16 +391,23 @@ void deflate_fixed(const uint8_t *d, size_t n, std::vector<uint8_t> &out)
             }
         }
         if (best >= 3) {
-            put_match(o, best, bestd);
-            for (int k = 0; k < best; ++k) insert(i + k);
+            o.put(fc.len_code[best], fc.len_bits[best]);
+            const int j = fc.dsym(bestd);
+            o.put(fc.dist_rev[j] | ((uint32_t)(bestd - kDistBase[j]) << 5), 5 + kDistExtra[j]);
+            if (best <= kMaxInsert) {
+                for (int k = 0; k < best; ++k) insert(i + k);
+            } else {
+                for (int k = 0; k < kMaxInsert; ++k) insert(i + k);
+                for (int k = best - kMaxInsert; k < best; ++k) insert(i + k);
+            }
             i += best;
         } else {
-            put_literal(o, d[i]);
+            o.put(fc.lit[d[i]], fc.lit_bits[d[i]]);
             insert(i);
             ++i;
         }
     }
-    put_literal(o, 256);
+    o.put(fc.lit[256], fc.lit_bits[256]);
     o.flush();
 }
 
@@ -523,37 +593,62 @@ bool decode(const uint8_t *d, size_t n, Image &img, std::string &err)
     return true;
 }
 
+// Row filter f of a 4-byte-per-pixel row into out (x - predictor, mod 256),
+// returning the sum of the filtered bytes as signed values, |(int8)v|: the
+// selection heuristic of the PNG specification. `up` is the previous row
+// (all zeros above the first). One straight loop per filter.
+long filter_row(int f, const uint8_t *row, const uint8_t *up, size_t stride, uint8_t *out)
+{
+    long sum = 0;
+    auto emit = [&](size_t i, int pred) {
+        const uint8_t v = (uint8_t)(row[i] - pred);
+        out[i] = v;
+        sum += std::abs((int)(int8_t)v);
+    };
+    const size_t head = std::min<size_t>(4, stride);
+    switch (f) {
+    case 0:
+        for (size_t i = 0; i < stride; ++i) emit(i, 0);
+        break;
+    case 1:
+        for (size_t i = 0; i < head; ++i) emit(i, 0);
+        for (size_t i = 4; i < stride; ++i) emit(i, row[i - 4]);
+        break;
+    case 2:
+        for (size_t i = 0; i < stride; ++i) emit(i, up[i]);
+        break;
+    case 3:
+        for (size_t i = 0; i < head; ++i) emit(i, up[i] >> 1);
+        for (size_t i = 4; i < stride; ++i) emit(i, (row[i - 4] + up[i]) >> 1);
+        break;
+    default:
+        for (size_t i = 0; i < head; ++i) emit(i, paeth(0, up[i], 0));
+        for (size_t i = 4; i < stride; ++i) emit(i, paeth(row[i - 4], up[i], up[i - 4]));
+        break;
+    }
+    return sum;
+}
+
 std::vector<uint8_t> encode(const uint8_t *rgba, int width, int height)
 {
     const size_t stride = (size_t)width * 4;
-    std::vector<uint8_t> filtered;
-    filtered.reserve((stride + 1) * height);
-    std::vector<uint8_t> cand(stride), best(stride);
+    std::vector<uint8_t> filtered((stride + 1) * height);
+    std::vector<uint8_t> cand(5 * stride), zero(stride, 0);
     for (int y = 0; y < height; ++y) {
         const uint8_t *row = rgba + (size_t)y * stride;
-        const uint8_t *up = y > 0 ? row - stride : nullptr;
+        const uint8_t *up = y > 0 ? row - stride : zero.data();
         long best_sum = -1;
         int best_f = 0;
         for (int f = 0; f < 5; ++f) {
-            long sum = 0;
-            for (size_t i = 0; i < stride; ++i) {
-                const int a = i >= 4 ? row[i - 4] : 0, b = up ? up[i] : 0, c = (up && i >= 4) ? up[i - 4] : 0;
-                int p = 0;
-                if (f == 1) p = a;
-                else if (f == 2) p = b;
-                else if (f == 3) p = (a + b) >> 1;
-                else if (f == 4) p = paeth(a, b, c);
-                cand[i] = (uint8_t)(row[i] - p);
-                sum += std::abs((int)(int8_t)cand[i]);
-            }
-            if (best_sum < 0 || sum < best_sum) {
+            const long sum = filter_row(f, row, up, stride, cand.data() + f * stride);
+            if (best_sum < 0 || sum < best_sum) {  // the first filter of least sum
                 best_sum = sum;
                 best_f = f;
-                best.swap(cand);
             }
         }
-        filtered.push_back((uint8_t)best_f);
-        filtered.insert(filtered.end(), best.begin(), best.end());
+        uint8_t *dst = filtered.data() + (size_t)y * (stride + 1);
+        dst[0] = (uint8_t)best_f;
+        std::memcpy(dst + 1, cand.data() + best_f * stride, stride);
     }
     std::vector<uint8_t> out = {137, 80, 78, 71, 13, 10, 26, 10};
     auto chunk = [&](const char *type, const std::vector<uint8_t> &data) {
