@@ -2,7 +2,6 @@
 Python writer / reader built on the stdlib zlib (no GPU)."""
 import os
 import struct
-import subprocess
 import zlib
 
 import numpy as np
@@ -120,17 +119,3 @@ def test_decode_rejects_bad_files():
     assert P.c_decode(b"not a png at all")[1] == "not a PNG file"
     ihdr16 = P._chunk(b"IHDR", struct.pack(">IIBBBBB", 5, 4, 16, 6, 0, 0, 0))  # 16-bit RGBA header
     assert P.c_decode(png[:8] + ihdr16 + png[8 + 25:])[1] == "16-bit PNGs are not supported"
-
-
-def test_cli_argument_checks():
-    """The driver's argument handling needs no GPU (src/main.cpp:110-126)."""
-    if not os.path.exists(P.CLI):
-        pytest.skip("driver not built")
-    r = subprocess.run([P.CLI], capture_output=True, text=True)
-    assert r.returncode == 1 and "Usage:" in r.stderr
-    r = subprocess.run([P.CLI, "0", "0.1", "0", "a.png", "b.png"], capture_output=True, text=True)
-    assert r.returncode == 1 and "Timesteps must be greater than 0." in r.stderr
-    r = subprocess.run([P.CLI, "3", "-1", "0", "a.png", "b.png"], capture_output=True, text=True)
-    assert r.returncode == 1 and "Delta T must be greater than 0." in r.stderr
-    r = subprocess.run([P.CLI, "3", "0.1", "0", "/nonexistent.png", "b.png"], capture_output=True, text=True)
-    assert r.returncode == 1 and "Something went wrong reading the input image" in r.stderr
