@@ -71,22 +71,41 @@ uint8_t to_byte(float x)
     return (uint8_t)v;  // truncation, as the reference's cast
 }
 
-// Encodes and writes the per-step PNGs on worker threads, so the steps go on
-// while earlier frames are compressed (the frames are independent). The queue
-// is bounded; the first failure is kept and reported by finish().
+// Converts, encodes and writes the per-step PNGs on worker threads, so the
+// steps go on while earlier frames are compressed (the frames are
+// independent). The queue is bounded; the first failure is kept and reported
+// by finish().
 class PngWriters {
   public:
     PngWriters(int width, int height, int threads, size_t max_queued)
-        : w_(width), h_(height), max_queued_(max_queued)
+        : w_(width), h_(height), max_queued_(max_queued), max_buffers_(max_queued + 2)
     {
         for (int k = 0; k < threads; ++k) pool_.emplace_back([this] { run(); });
     }
     ~PngWriters() { finish(); }
-    void submit(std::string path, std::vector<uint8_t> rgba)
+    // A frame buffer of n floats: one the workers have finished with, or a new
+    // one while fewer than max_queued + 2 exist (else wait for one: a worker
+    // hands its frame back as soon as it has converted it to bytes).
+    std::vector<float> take_buffer(size_t n)
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        buf_.wait(lk, [this] { return !free_.empty() || allocated_ < max_buffers_; });
+        if (!free_.empty()) {
+            std::vector<float> b = std::move(free_.back());
+            free_.pop_back();
+            b.resize(n);
+            return b;
+        }
+        ++allocated_;
+        lk.unlock();
+        return std::vector<float>(n);
+    }
+    // `image`: the step's image as floats, converted to bytes on the worker
+    void submit(std::string path, std::vector<float> image)
     {
         std::unique_lock<std::mutex> lk(mu_);
         room_.wait(lk, [this] { return jobs_.size() < max_queued_; });
-        jobs_.push_back({std::move(path), std::move(rgba)});
+        jobs_.push_back({std::move(path), std::move(image)});
         work_.notify_one();
     }
     // Waits for every frame; returns the first error message ("" if none).
@@ -106,7 +125,7 @@ class PngWriters {
   private:
     struct Job {
         std::string path;
-        std::vector<uint8_t> rgba;
+        std::vector<float> image;
     };
     void run()
     {
@@ -120,19 +139,27 @@ class PngWriters {
                 jobs_.pop_front();
                 room_.notify_one();
             }
+            std::vector<uint8_t> rgba(j.image.size());
+            for (size_t k = 0; k < rgba.size(); ++k) rgba[k] = to_byte(j.image[k]);
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                free_.push_back(std::move(j.image));  // for the next step's frame
+            }
+            buf_.notify_one();
             std::string err;
-            if (!pfs::png::write_file(j.path, j.rgba.data(), w_, h_, err)) {
+            if (!pfs::png::write_file(j.path, rgba.data(), w_, h_, err)) {
                 std::lock_guard<std::mutex> lk(mu_);
                 if (error_.empty()) error_ = err;
             }
         }
     }
     int w_, h_;
-    size_t max_queued_;
+    size_t max_queued_, max_buffers_, allocated_ = 0;
     std::vector<std::thread> pool_;
     std::deque<Job> jobs_;
+    std::vector<std::vector<float>> free_;
     std::mutex mu_;
-    std::condition_variable work_, room_;
+    std::condition_variable work_, room_, buf_;
     bool closing_ = false;
     std::string error_;
 };
@@ -208,18 +235,20 @@ int main(int argc, char *argv[])
     std::printf("Simulating [%d x %d] domain for %d timesteps at dt=%g...\n", velocity.height, velocity.width,
                 n_timesteps, (double)delta_t);
     const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    PngWriters writers(input.width, input.height, write ? nthreads : 0, 2 * (size_t)nthreads);
+    // frames waiting for a writer: up to two per thread, and about 512 MB of them at most
+    const size_t frame_bytes = std::max<size_t>(1, image.size() * sizeof(float));
+    const size_t queue = std::max<size_t>(1, std::min<size_t>(2 * (size_t)nthreads, (512u << 20) / frame_bytes));
+    PngWriters writers(input.width, input.height, write ? nthreads : 0, queue);
     const auto t0 = std::chrono::high_resolution_clock::now();
     for (int i = 0; i < n_timesteps; ++i) {
         if (pfs_session_step(s, 1) != PFS_OK) return fail_api("pfs_session_step");
         if (write) {
-            if (pfs_session_download(s, nullptr, nullptr, image.data(), PFS_HOST) != PFS_OK)
+            std::vector<float> frame = writers.take_buffer(image.size());
+            if (pfs_session_download(s, nullptr, nullptr, frame.data(), PFS_HOST) != PFS_OK)
                 return fail_api("pfs_session_download");
-            std::vector<uint8_t> bytes(image.size());
-            for (size_t k = 0; k < image.size(); ++k) bytes[k] = to_byte(image[k]);
             std::string path = std::string(argv[6]) + "/" + std::to_string(i) + ".png";
             std::printf("[%d] Writing to : %s\n", i, path.c_str());
-            writers.submit(std::move(path), std::move(bytes));
+            writers.submit(std::move(path), std::move(frame));
         }
     }
     if (pfs_session_sync(s) != PFS_OK) return fail_api("pfs_session_sync");
