@@ -22,6 +22,7 @@
 #include <utility>
 
 #include "kernels.h"
+#include "nvtx.h"
 #include "pfs.h"
 #include "precision.h"
 #include "unet.h"
@@ -261,6 +262,7 @@ struct CheckPoint {
 // no role refers to.
 int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStream_t st, int &cur, int &prev)
 {
+    pfs::NvtxRange range("pfs.pressure");
     cur = f.pidx[X];
     prev = f.pidx[Y];
     int freep = 3 - cur - prev;
@@ -389,6 +391,7 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
 // reference's vp) are set; the caller projects Z -> W.
 int velocity_phase(Field &f, int vp, int tmp, const StepCfg &c, StepOut &o, cudaStream_t st, int &Z, int &W)
 {
+    pfs::NvtxRange range("pfs.velocity");
     const int A = vp, B = tmp;
     // advect(vp, tmp): src/fluid.cpp:300
     CK(pfs::launch_advect(f.u[A], f.v[A], f.u[B], f.v[B], f.ld, f.w, f.h, c.dt, st, c.bc));
@@ -661,6 +664,7 @@ int pfs_release_workspace(void)
 
 int pfs_simulate_fluid_step(float **vp, float **tmp, float dt, float viscosity, int vx, int vy, int vz)
 {
+    pfs::NvtxRange range("pfs.simulate_fluid_step");
     if (!vp || !tmp || !*vp || !*tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "null buffer");
     if (*vp == *tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "vp and tmp must be distinct buffers");
     CKS(check_dims(vx, vy, vz, dt));
@@ -995,6 +999,7 @@ static int io_init(pfs_session *s)
 
 int pfs_session_upload_async(pfs_session *s, const float *vp, const float *tmp, const float *image)
 {
+    pfs::NvtxRange range("pfs.upload_async");
     if (!s || !vp || !tmp) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
     if (s->ic > 0 && !image) return fail(PFS_ERR_INVALID_ARGUMENT, "session has an image: pass it");
     if (s->up_count == PFS_IO_SLOTS)
@@ -1030,6 +1035,7 @@ static int apply_queued_upload(pfs_session *s)
 
 int pfs_session_download_async(pfs_session *s, float *vp, float *tmp, float *image)
 {
+    pfs::NvtxRange range("pfs.download_async");
     if (!s) return fail(PFS_ERR_INVALID_ARGUMENT, "null session");
     CKS(io_init(s));
     const size_t vcount = (size_t)s->f.w * s->f.h * 4, icount = (size_t)s->iw * s->ih * s->ic;
@@ -1074,6 +1080,7 @@ int pfs_session_step(pfs_session *s, int n)
         lp.coarsen = s->net_coarsen;
         lp.passes = s->net_passes;
         for (int k = 0; k < n; ++k) {
+            pfs::NvtxRange range("pfs.step");
             pfs::LpOut o;
             CKS(pfs::lp_step(s->lp, lp, s->st, o));
             s->stats.start_kind = o.start_kind;
@@ -1093,9 +1100,11 @@ int pfs_session_step(pfs_session *s, int n)
     Field &f = s->f;
     const StepCfg c = session_cfg(s);
     for (int k = 0; k < n; ++k) {
+        pfs::NvtxRange range("pfs.step");
         StepOut o;
         int Z, W;
         CKS(velocity_phase(f, s->vpSlot, s->tmpSlot, c, o, s->st, Z, W));
+        pfs::NvtxRange project_range("pfs.project_image");
         const float *pz = f.p[f.pidx[Z]];
         if (s->ic > 0 && s->iw == f.w && s->ih == f.h) {
             float *src = s->img[s->icur], *dst = s->img[1 - s->icur];

@@ -29,6 +29,7 @@
 
 #include "cells.cuh"
 #include "kernels.h"
+#include "nvtx.h"
 #include "pfs.h"
 #include "reduce.cuh"
 #include "sweep_stream.cuh"
@@ -702,6 +703,7 @@ int pfs_ensemble_upload(pfs_ensemble *e, int k, const float *vp, const float *tm
 
 int pfs_ensemble_step(pfs_ensemble *e, int steps)
 {
+    pfs::NvtxRange range("pfs.ensemble_step");
     Ensemble *E = reinterpret_cast<Ensemble *>(e);
     if (!E || steps < 0) return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "bad ensemble step arguments");
     if (E->graphs_ok && !E->graph[0]) {
