@@ -1,0 +1,82 @@
+// The fused sweep kernel template and its launch helpers, shared by the
+// translation units that instantiate it (sweep_kernels.cu: float sweeps;
+// sweep_check_kernels.cu: the check launches; sweep_lp_kernels.cu: 16-bit
+// storage). Split so that the many instantiations compile in parallel.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.h"
+#include "storage.cuh"
+#include "sweep_stream.cuh"
+
+namespace pfs {
+
+namespace {
+
+// RES: the launch ends a check interval. Every block (also one whose warps
+// have no task) adds its stored cells' squared residual of level L, and the
+// grid reduction records the check in a.state (done at or below a.tol), as
+// the residual kernels do. `done` is set before the launch starts, so either
+// every block returns at once or none does.
+template <typename T, int G, int L, bool PREV, bool RES = false>
+__global__ void __launch_bounds__(128, RES && L >= 5 ? 2 : min_blocks<L>()) k_sweep_stream(StreamArgs<T> a)
+{
+    using V = typename Store<T>::Vec;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    V *sm_rings = reinterpret_cast<V *>(sm_raw);
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int wid = blockIdx.x * 4 + wib;
+    if constexpr (!RES) {
+        if (wid >= a.nwork) return;  // whole warp
+        if (a.done && *(volatile const int *)a.done) return;
+        stream_task<T, G, L, PREV>(a, wid, lane, sm_rings + wib * Ring<T, L>::vecs_per_warp);
+    } else {
+        if (a.done && *(volatile const int *)a.done) return;  // the whole grid
+        FFAcc2 acc[2];
+        if (wid < a.nwork)
+            stream_task<T, G, L, PREV, true>(a, wid, lane, sm_rings + wib * Ring<T, L, true>::vecs_per_warp, acc);
+        reduce_blocks(acc[0].value() + acc[1].value(), a.red, 0, a.state, a.sweeps_here, a.tol);
+    }
+}
+
+template <typename T, int G, int L, bool PREV, bool RES = false>
+cudaError_t launch_stream_t(const StreamArgs<T> &a, cudaStream_t st)
+{
+    constexpr int smem = Ring<T, L, RES>::bytes_per_block;
+    static std::atomic<unsigned long long> attr_done{0};  // per instantiation and device
+    const cudaError_t e = smem_limit_once(k_sweep_stream<T, G, L, PREV, RES>, smem, attr_done);
+    if (e != cudaSuccess) return e;
+    const int blocks = (a.nwork + 3) / 4;  // 4 warps per block: the shared rings are laid out for 4
+    if (RES && blocks > a.red.nblocks) return cudaErrorInvalidValue;
+    k_sweep_stream<T, G, L, PREV, RES><<<blocks, 128, smem, st>>>(a);
+    return launched();
+}
+
+template <typename T, int G, int L>
+cudaError_t launch_stream_l(const StreamArgs<T> &a, bool prev, cudaStream_t st)
+{
+    return prev ? launch_stream_t<T, G, L, true>(a, st) : launch_stream_t<T, G, L, false>(a, st);
+}
+
+template <typename T>
+StreamArgs<T> stream_args(const T *pin, const T *b, T *pout, T *pprev, int ld, int w, int h, int halo, int chunk,
+                          const int *done)
+{
+    StreamArgs<T> a{};
+    a.pin = pin;
+    a.b = b;
+    a.pout = pout;
+    a.pprev = pprev;
+    a.done = done;
+    a.ld = ld;
+    a.w = w;
+    a.h = h;
+    a.chunk = chunk;
+    a.nsx = (w + 128 - 2 * halo - 1) / (128 - 2 * halo);
+    a.nwork = a.nsx * ((h + chunk - 1) / chunk);
+    return a;
+}
+
+}  // namespace
+
+}  // namespace pfs
