@@ -65,7 +65,8 @@ int pfs_set_jacobi_iters(int n);
 int pfs_get_jacobi_iters(void);
 /* Stream for the drop-in calls below (a cudaStream_t, NULL = legacy default). */
 int pfs_set_stream(void *stream);
-/* Free the cached scratch of the drop-in calls on the current device. */
+/* Free the cached scratch of the drop-in calls and of pfs_residual_norms on
+ * the current device. */
 int pfs_release_workspace(void);
 
 /* ---- drop-in: CUDA branch of includes/fluid.hpp -------------------------------- */
@@ -152,7 +153,13 @@ enum { PFS_HOST = 0, PFS_DEVICE = 1 };
  * reference's buffer roles then reduce to: pressure iteration from the
  * previous final pressure, projection with the final pressure); other
  * settings return PFS_ERR_UNSUPPORTED. check_every sets the sweeps between
- * refinements of the refined forms (0 means 32). */
+ * refinements of the refined forms (0 means 32), except for F32R in residual
+ * mode (tol > 0): there the correction sweeps run with the F32 form's fused
+ * residual checks every check_every sweeps, and the FP64 refinement runs when
+ * the correction's residual reaches the tolerance or every 0.025 * n^2 sweeps
+ * (n the larger grid side; long before the float32 correction nears its
+ * rounding floor), so the refinement pass is rare and the sweeps run at the F32
+ * form's rate. */
 enum { PFS_PREC_F32 = 0, PFS_PREC_BF16 = 1, PFS_PREC_F16 = 2, PFS_PREC_F64 = 3, PFS_PREC_F32R = 4 };
 
 typedef struct {
@@ -167,6 +174,13 @@ typedef struct {
     int want_residual;  /* fixed mode: also report the final residual              */
     int precision;      /* PFS_PREC_*                                              */
     int boundary;       /* PFS_BOUNDARY_* (sessions of the F32 form)               */
+    int stall_sweeps;   /* residual mode: end the solve when the relative residual
+                           has not fallen below 0.99 x its lowest value for this
+                           many sweeps (the iterate has reached the rounding floor
+                           of its storage; stats.stalled); < 0 picks a window
+                           from the grid size, long enough that the exact
+                           iteration's slowest mode falls 3% within it; 0 (the
+                           default) never stops early                            */
 } pfs_params;
 
 /* Boundary mode of the advection (velocity and image):
@@ -196,6 +210,8 @@ typedef struct {
     int start_kind;      /* initial pressure of the last step: PFS_START_* */
     double rel_start;    /* relative residual of that initial pressure (-1 if not evaluated) */
     int start_passes;    /* damped passes applied to a predicted start in the last step    */
+    int stalled;         /* last step ended because its residual stopped falling
+                            (pfs_params.stall_sweeps)                                     */
 } pfs_stats;
 
 typedef struct pfs_session pfs_session;
@@ -370,7 +386,12 @@ int pfs_ensemble_destroy(pfs_ensemble *e);
  */
 int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *p_prev, int vx, int vy, int ld,
                         int levels, int fused, int chunk_rows, void *stream);
-/* ||b - A p||_2^2 and ||b||_2^2 (FP64) of planar p, b; blocking. */
+/* ||b - A p||_2^2 and ||b||_2^2 (FP64) of planar p, b; blocking. The
+ * reduction's scratch (about 10 KB per device, any grid size) is allocated on
+ * the first call on a device and kept until pfs_release_workspace(). Any
+ * pointer alignment is accepted: 16-byte aligned planes with vx and ld
+ * multiples of 4 take a vector-load kernel, others a scalar one (the sums agree
+ * to rounding). */
 int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, double *rr, double *bb,
                        void *stream);
 
@@ -382,7 +403,7 @@ int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, d
  * caching pool that owns the device) would get out-of-memory from cudaMalloc,
  * and a caller on a latency-critical path cannot afford cudaMalloc, which may
  * synchronize the device. pfs_residual_norms allocates its scratch on first use
- * per device and grid size; this call allocates nothing.
+ * per device; this call allocates nothing.
  *
  * Same kernel and same results as pfs_residual_norms. Its cross-block scratch
  * is a fixed 10 KiB array inside the library, present on every device that

@@ -152,9 +152,9 @@ struct Field {
         red.partials = rmem;
         red.result = rmem + 2 * nb;
         red.ticket = ticket;
-        red.nblocks = nb;
+        red.nblocks = pfs::reduce_grid();
         // capacity for the fused check launches at chunks of 16 rows or more
-        const int ns = std::max(nb, pfs::sweep_stream_blocks(w, h, 16));
+        const int ns = std::max(red.nblocks, pfs::sweep_stream_blocks(w, h, 16));
         CK(cudaMalloc(&psweep, 2 * (size_t)ns * sizeof(double)));
         red_sweep = red;
         red_sweep.partials = psweep;
@@ -206,6 +206,7 @@ struct StepCfg {
     pfs::unet::Net *net = nullptr;
     int coarsen = 1, passes = 1;  // predicted start: coarsening of the network's grid, network applications
     int bc = PFS_BOUNDARY_PERIODIC;  // boundary mode of the advection (pfs_params.boundary)
+    int stall_window = 0;  // residual mode: sweeps without a 1% fall that end the solve (0: never)
 };
 
 struct StepOut {
@@ -215,6 +216,7 @@ struct StepOut {
     int start_kind = PFS_START_PREVIOUS;
     double rel_start = -1.0;
     int start_passes = 0;
+    bool stalled = false;
 };
 
 bool fused_ok(const Field &f) { return f.w % 4 == 0; }
@@ -314,7 +316,8 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
             if (pending && (since >= 1 || last)) CKS(settle());
             if (check_fused && last)
                 CK(pfs::launch_sweep_stream_check(f.p[cur], f.b, f.p[freep], f.p[prev], f.ld, f.w, f.h, n,
-                                                  c.tun.chunk, f.red_sweep, f.dstate, S + n, c.tol, done, st));
+                                                  c.tun.chunk, f.red_sweep, f.dstate, S + n, c.tol, done, st,
+                                                  c.stall_window));
             else
                 CK(pfs::launch_sweep_stream(f.p[cur], f.b, f.p[freep], last ? f.p[prev] : nullptr, f.ld, f.w, f.h,
                                             n, c.tun.halo, c.tun.chunk, done, st));
@@ -328,7 +331,7 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
         if (!check_fused) {
             CK(cudaEventRecord(f.ev_check, st));
             CK(cudaStreamWaitEvent(f.aux, f.ev_check, 0));
-            CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, f.aux));
+            CK(pfs::launch_residual(f.p[cur], f.b, f.ld, f.w, f.h, f.red, f.dstate, S, c.tol, f.aux, c.stall_window));
             CK(cudaEventRecord(f.ev_res, f.aux));
             pending = true;
             since = 0;
@@ -370,7 +373,8 @@ int pressure_solve(Field &f, int X, int Y, const StepCfg &c, StepOut &o, cudaStr
         }
     }
     o.sweeps = S;
-    o.capped = resid && S == c.S && !(o.rel <= c.tol);
+    o.stalled = resid && nmarks > 0 && f.hstate->done == 2;
+    o.capped = resid && S == c.S && !(o.rel <= c.tol) && !o.stalled;
     // a solve that ran to the cap is likely followed by another: enqueue all its checks in one batch
     // (one host read of the state instead of five for 20 checks); any converged solve resets to
     // doubling from 1, so at most one step after a change enqueues intervals that return at once
@@ -501,6 +505,49 @@ int get_workspace(int w, int h, Workspace **out)
     return PFS_OK;
 }
 
+// Scratch of pfs_residual_norms: the reduction's per-block partials, results
+// and tickets (about 10 KB) and a pinned result pair, one set per device,
+// sized for any grid; kept apart from the drop-in step's planar workspace so
+// that norms at one grid size never reallocate the step's scratch.
+struct NormScratch {
+    double *rmem = nullptr;
+    double *hres = nullptr;
+    pfs::Reduce red{};
+    ~NormScratch()
+    {
+        if (rmem) cudaFree(rmem);
+        if (hres) cudaFreeHost(hres);
+    }
+};
+std::map<int, NormScratch *> g_norms;  // keyed by device
+
+int get_norm_scratch(NormScratch **out)
+{
+    int dev;
+    CK(cudaGetDevice(&dev));
+    NormScratch *&ns = g_norms[dev];
+    if (!ns) {
+        NormScratch *n = new (std::nothrow) NormScratch();
+        if (!n) return fail(PFS_ERR_CUDA, "out of host memory");
+        const int nb = pfs::kReduceBlocks;
+        const size_t bytes = (2 * nb + 2) * sizeof(double) + 16;
+        cudaError_t e = cudaMalloc(&n->rmem, bytes);
+        if (e == cudaSuccess) e = cudaMemset(n->rmem, 0, bytes);
+        if (e == cudaSuccess) e = cudaMallocHost(&n->hres, 2 * sizeof(double));
+        if (e != cudaSuccess) {
+            delete n;
+            return fail(PFS_ERR_CUDA, "norm scratch: %s", cudaGetErrorString(e));
+        }
+        n->red.partials = n->rmem;
+        n->red.result = n->rmem + 2 * nb;
+        n->red.ticket = reinterpret_cast<unsigned *>(n->rmem + 2 * nb + 2);
+        n->red.nblocks = pfs::reduce_grid();
+        ns = n;
+    }
+    *out = ns;
+    return PFS_OK;
+}
+
 int check_dims(int vx, int vy, int vz, float dt)
 {
     if (vx <= 0 || vy <= 0) return fail(PFS_ERR_INVALID_ARGUMENT, "grid %dx%d must be positive", vx, vy);
@@ -623,7 +670,7 @@ const char *pfs_status_string(int s)
 
 const char *pfs_last_error(void) { return g_err.c_str(); }
 
-int pfs_version(void) { return 100; }
+int pfs_version(void) { return 200; }
 
 long long pfs_kernel_launches(void) { return pfs::g_launches.load(std::memory_order_relaxed); }
 
@@ -658,6 +705,12 @@ int pfs_release_workspace(void)
         CK(cudaDeviceSynchronize());
         delete it->second;
         g_ws.erase(it);
+    }
+    auto jt = g_norms.find(dev);
+    if (jt != g_norms.end()) {
+        CK(cudaDeviceSynchronize());
+        delete jt->second;
+        g_norms.erase(jt);
     }
     return PFS_OK;
 }
@@ -771,6 +824,7 @@ void pfs_params_default(pfs_params *p)
     p->chunk_rows = 0;
     p->want_residual = 0;
     p->boundary = PFS_BOUNDARY_PERIODIC;
+    p->stall_sweeps = 0;
 }
 
 static int check_params(const pfs_params *p)
@@ -810,12 +864,15 @@ static StepCfg session_cfg(const pfs_session *s)
     c.want_res = s->prm.want_residual != 0;
     if (s->prm.fuse_depth > 0) c.tun.levels = s->prm.fuse_depth;
     c.tun.halo = c.tun.levels <= 4 ? 4 : 8;
-    if (s->prm.chunk_rows > 0) c.tun.chunk = s->prm.chunk_rows;
+    c.tun.chunk = s->prm.chunk_rows > 0 ? s->prm.chunk_rows : pfs::default_chunk(s->f.w, s->f.h, c.tun.levels);
     c.start_mode = s->start_mode;
     c.net = s->net;
     c.coarsen = s->net_coarsen;
     c.passes = s->net_passes;
     c.bc = s->prm.boundary;
+    if (c.tol > 0.0 && s->prm.stall_sweeps != 0)
+        c.stall_window = s->prm.stall_sweeps > 0 ? s->prm.stall_sweeps
+                                                 : pfs::auto_stall_window(std::max(s->f.w, s->f.h), c.check_every);
     return c;
 }
 
@@ -1074,11 +1131,16 @@ int pfs_session_step(pfs_session *s, int n)
         lp.tol = s->prm.tol;
         lp.check_every = s->prm.check_every;
         lp.levels = s->prm.fuse_depth > 0 ? s->prm.fuse_depth : 8;
-        lp.chunk = s->prm.chunk_rows > 0 ? s->prm.chunk_rows : 32;
+        lp.chunk = s->prm.chunk_rows > 0 ? s->prm.chunk_rows : pfs::default_chunk(s->f.w, s->f.h, lp.levels);
         lp.start_mode = s->start_mode;
         lp.net = s->net;
         lp.coarsen = s->net_coarsen;
         lp.passes = s->net_passes;
+        if (lp.tol > 0.0 && s->prm.stall_sweeps != 0)
+            lp.stall_window = s->prm.stall_sweeps > 0
+                                  ? s->prm.stall_sweeps
+                                  : pfs::auto_stall_window(std::max(s->f.w, s->f.h),
+                                                           lp.check_every > 0 ? lp.check_every : 32);
         for (int k = 0; k < n; ++k) {
             pfs::NvtxRange range("pfs.step");
             pfs::LpOut o;
@@ -1091,6 +1153,7 @@ int pfs_session_step(pfs_session *s, int n)
             s->stats.rel_residual = o.rel;
             s->stats.bnorm = o.bnorm;
             s->stats.capped = o.capped ? 1 : 0;
+            s->stats.stalled = o.stalled ? 1 : 0;
             s->stats.steps += 1;
             s->stats.total_sweeps += o.sweeps;
             s->stats.cap_hits += o.capped ? 1 : 0;
@@ -1127,6 +1190,7 @@ int pfs_session_step(pfs_session *s, int n)
         s->stats.rel_residual = o.rel;
         s->stats.bnorm = o.bnorm;
         s->stats.capped = o.capped ? 1 : 0;
+        s->stats.stalled = o.stalled ? 1 : 0;
         s->stats.steps += 1;
         s->stats.total_sweeps += o.sweeps;
         s->stats.cap_hits += o.capped ? 1 : 0;
@@ -1267,7 +1331,7 @@ int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *
         if (levels > 8) return fail(PFS_ERR_UNSUPPORTED, "fused sweeps: at most 8 levels per call");
         const int halo = levels <= 4 ? 4 : 8;
         CK(pfs::launch_sweep_stream(p_in, b, p_out, p_prev, ld, vx, vy, levels, halo,
-                                    chunk_rows > 0 ? chunk_rows : 32, nullptr, st));
+                                    chunk_rows > 0 ? chunk_rows : pfs::default_chunk(vx, vy, levels), nullptr, st));
         return PFS_OK;
     }
     if (levels > 1 && !p_prev) return fail(PFS_ERR_INVALID_ARGUMENT, "unfused multi-sweep needs p_prev as scratch");
@@ -1286,15 +1350,14 @@ int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, d
     if (!p || !b || !rr || !bb) return fail(PFS_ERR_INVALID_ARGUMENT, "null argument");
     if (vx <= 0 || vy <= 0 || ld < vx) return fail(PFS_ERR_INVALID_ARGUMENT, "bad dims");
     std::lock_guard<std::mutex> lk(g_mu);
-    Workspace *ws;
-    CKS(get_workspace(vx, vy, &ws));
+    NormScratch *ns;
+    CKS(get_norm_scratch(&ns));
     cudaStream_t st = (cudaStream_t)stream;
-    Field &f = ws->f;
-    CK(pfs::launch_norms(p, b, ld, vx, vy, f.red, st));
-    CK(cudaMemcpyAsync(f.hres, f.red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(pfs::launch_norms(p, b, ld, vx, vy, ns->red, st));
+    CK(cudaMemcpyAsync(ns->hres, ns->red.result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    *rr = f.hres[0];
-    *bb = f.hres[1];
+    *rr = ns->hres[0];
+    *bb = ns->hres[1];
     return PFS_OK;
 }
 

@@ -40,9 +40,12 @@ namespace {
 struct Member {
     int w, h, ld;
     float *u[2], *v[2];  // [0] current velocity, [1] advected
-    float *p[2];         // pressure ping-pong
-    float *b;
+    float *p[2];         // pressure ping-pong (the refined form: the float32 correction e)
+    float *b;            // divergence (the refined form: the correction's right-hand side r = b - A x)
     float *img[2];       // image ping-pong, c planes of ld*h each
+    double *x[2];        // the refined form: FP64 pressure and its damped-pass partner (else null)
+    float *bx;           // the refined form: the divergence b (else null)
+    int interval;        // the refined form: sweeps between refinements (f32r_refine_interval)
     int row_task0, nrow;     // row tasks (8 rows): advect, divergence, projection + image
     int sw_task0, nsx, nsy;  // fused sweep tasks
     int rs_task0, rsx, rsy;  // residual strip tasks
@@ -54,9 +57,15 @@ struct MemberState {
     int sweeps;   // sweeps of this step
     int checks;   // residual evaluations of this step
     int capped;
-    int pad;
+    int stalled;  // the refined form: the residual stopped falling
     double rel;   // last relative residual
     double bb;    // sum b^2
+    // the refined form
+    int zero_phase;    // sweep phase whose input correction is zero (the first after a refinement)
+    int refine_start;  // sweeps of this step at the last refinement
+    int refine;        // refine at the end of this check
+    int refines;       // refinements of this step
+    double last_rel;   // relative residual at the last refinement
 };
 
 struct EnsArgs {
@@ -69,6 +78,7 @@ struct EnsArgs {
     unsigned *bar_count, *bar_gen;
     int *err;
     int *active;  // members still iterating, one counter per check
+    int *refining;  // the refined form: members refining, one counter per check
     float dt, gamma;
     double tol;
     int cap, check_every, chunk, channels, icur;
@@ -124,7 +134,52 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-template <int G, int L>
+// The refined form's FP64 pieces, with the arithmetic of the refined
+// float32 session form (precision.cu: k_lp_refine, k_lp_damp, k_lp_project).
+// r = b - A x for cell (i, j): b + xL + xR + xT + xB - 4 x, in FP64.
+__device__ __forceinline__ double ref_residual(const double *__restrict__ x, const float *__restrict__ b, int ld, int w,
+                                               int h, int i, int j)
+{
+    const size_t r = (size_t)j * ld;
+    double q = __dadd_rn((double)__ldcg(b + r + i), __ldcg(x + r + wm(i, w)));
+    q = __dadd_rn(q, __ldcg(x + r + wp(i, w)));
+    q = __dadd_rn(q, __ldcg(x + (size_t)wm(j, h) * ld + i));
+    q = __dadd_rn(q, __ldcg(x + (size_t)wp(j, h) * ld + i));
+    return __fma_rn(-4.0, __ldcg(x + r + i), q);
+}
+
+// Projection with the FP64 pressure, ((x_R - x_L) rounded to float) * dt / 2,
+// then image advection with the projected velocity (as project_image_cell).
+__device__ __forceinline__ void ref_project_image_cell(const float *__restrict__ u, const float *__restrict__ v,
+                                                       const double *__restrict__ x, float *__restrict__ uo,
+                                                       float *__restrict__ vo, float *__restrict__ pout, int ld, int w,
+                                                       int h, float dt, const float *__restrict__ img,
+                                                       float *__restrict__ imgo, size_t plane, int c, int i, int j)
+{
+    const size_t r = (size_t)j * ld, o = r + i;
+    const float dx = (float)(__ldcg(x + r + wp(i, w)) - __ldcg(x + r + wm(i, w)));
+    const float dy = (float)(__ldcg(x + (size_t)wp(j, h) * ld + i) - __ldcg(x + (size_t)wm(j, h) * ld + i));
+    const float un = fsub(u[o], fdiv(fmul(dx, dt), 2.0f));
+    const float vn = fsub(v[o], fdiv(fmul(dy, dt), 2.0f));
+    uo[o] = un;
+    vo[o] = vn;
+    pout[o] = (float)__ldcg(x + o);  // the pressure in float32, for downloads
+    const Corners k = backtrace<0>(i, j, dt, dt, un, vn, (float)w, (float)h, w, h);
+    const size_t r0 = (size_t)k.j0 * ld, r1 = (size_t)k.j1 * ld;
+    for (int ch = 0; ch < c; ++ch) {
+        const float *sp = img + ch * plane;
+        imgo[ch * plane + o] = bilerp(k.sx, k.sy, sp[r0 + k.i0], sp[r0 + k.i1], sp[r1 + k.i0], sp[r1 + k.i1]);
+    }
+}
+
+// One timestep of every member. REF: the refined float32 form (PFS_PREC_F32R):
+// the sweeps iterate a float32 correction e on A e = r, r = b - A x, with the
+// pressure x in FP64; at check points a member whose estimate
+// ||r - A e|| / ||b|| is below the tolerance, or whose correction has run
+// `interval` sweeps, is refined: x += e, PFS_START_DAMP_PASSES damped FP64
+// passes (which remove the rounding noise in the modes Jacobi cannot damp),
+// then r = b - A x and the FP64 residual decides.
+template <int G, int L, bool REF>
 __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
 {
     extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -145,14 +200,14 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
     }
     if (!grid_sync(a)) return;
 
-    // divergence of the advected velocity, b^2 per task
+    // divergence of the advected velocity (the refined form: into bx), b^2 per task
     for (int t = gw; t < a.nrow_tasks; t += nw) {
         const Member &m = a.mem[a.row_member[t]];
         const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
         FFAcc acc;
         for (int j = r0; j < r1; ++j)
             for (int i = lane; i < m.w; i += 32)
-                acc_square(acc, divergence_cell(m.u[1], m.v[1], m.b, m.ld, m.w, m.h, a.gamma, i, j));
+                acc_square(acc, divergence_cell(m.u[1], m.v[1], REF ? m.bx : m.b, m.ld, m.w, m.h, a.gamma, i, j));
         const double s = warp_sum(acc.value());
         if (lane == 0) a.row_part[t] = s;
     }
@@ -167,8 +222,47 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         ms.sweeps = 0;
         ms.checks = 0;
         ms.capped = 0;
+        ms.stalled = 0;
+        if (REF) {
+            ms.cur = 0;
+            ms.zero_phase = 0;
+            ms.refine_start = 0;
+            ms.refine = 0;
+            ms.refines = 0;
+        }
     }
     if (!grid_sync(a)) return;
+
+    if (REF) {
+        // the residual of the starting pressure (the previous step's x): r = b - A x into m.b
+        for (int t = gw; t < a.nrow_tasks; t += nw) {
+            const Member &m = a.mem[a.row_member[t]];
+            const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+            double acc = 0.0;
+            for (int j = r0; j < r1; ++j)
+                for (int i = lane; i < m.w; i += 32) {
+                    const double q = ref_residual(m.x[0], m.bx, m.ld, m.w, m.h, i, j);
+                    m.b[(size_t)j * m.ld + i] = (float)q;
+                    acc = __fma_rn(q, q, acc);
+                }
+            acc = warp_sum(acc);
+            if (lane == 0) a.row_part[t] = acc;
+        }
+        if (!grid_sync(a)) return;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+            const Member &m = a.mem[k];
+            double rr = 0.0;
+            for (int t = 0; t < m.nrow; ++t) rr += __ldcg(a.row_part + m.row_task0 + t);
+            volatile MemberState &ms = a.state[k];
+            const double bb = ms.bb;
+            const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
+            ms.rel = rel;
+            ms.last_rel = rel;
+            ms.checks = 1;
+            if (rel <= a.tol) ms.done = 1;  // already converged: no sweeps
+        }
+        if (!grid_sync(a)) return;
+    }
 
     // pressure: phases of L fused sweeps; residual checks every check_every sweeps and at the cap
     int phase = 0, check = 0;
@@ -179,7 +273,7 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             const int cur = vload(a.state[mi].cur);
             const Member &m = a.mem[mi];
             StreamArgs<float> sa;
-            sa.pin = m.p[(cur + phase) & 1];
+            sa.pin = (REF && vload(a.state[mi].zero_phase) == phase) ? nullptr : m.p[(cur + phase) & 1];
             sa.pout = m.p[(cur + phase + 1) & 1];
             sa.b = m.b;
             sa.pprev = nullptr;
@@ -217,8 +311,18 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             for (int t = 0; t < m.rsx * m.rsy; ++t) rr += __ldcg(a.rs_part + m.rs_task0 + t);
             const double bb = ms.bb;
             const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
-            ms.rel = rel;
             ms.checks = ms.checks + 1;
+            if (REF) {
+                // the estimate of x + e's residual: refine when it meets the tolerance, when the
+                // correction has run its interval, or at the cap
+                if (rel <= 0.999 * a.tol || s - ms.refine_start >= m.interval || s == a.cap) {
+                    ms.refine = 1;
+                    atomicAdd(a.refining + check, 1);
+                }
+                atomicAdd(a.active + check, 1);
+                continue;
+            }
+            ms.rel = rel;
             if (rel <= a.tol || s == a.cap) {
                 ms.done = 1;
                 ms.sweeps = s;
@@ -229,6 +333,81 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             }
         }
         if (!grid_sync(a)) return;
+        if (REF && *(volatile int *)(a.refining + check) > 0) {
+            // x += e for the refining members
+            for (int t = gw; t < a.nrow_tasks; t += nw) {
+                const int mi = a.row_member[t];
+                if (!vload(a.state[mi].refine)) continue;
+                const Member &m = a.mem[mi];
+                const float *e = m.p[(vload(a.state[mi].cur) + phase) & 1];
+                const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+                for (int j = r0; j < r1; ++j)
+                    for (int i = lane; i < m.w; i += 32) {
+                        const size_t o = (size_t)j * m.ld + i;
+                        m.x[0][o] = __dadd_rn(__ldcg(m.x[0] + o), (double)__ldcg(e + o));
+                    }
+            }
+            if (!grid_sync(a)) return;
+            // damped passes x += (b - A x) / 8, x[0] -> x[1] -> x[0] ...
+            for (int pass = 0; pass < PFS_START_DAMP_PASSES; ++pass) {
+                for (int t = gw; t < a.nrow_tasks; t += nw) {
+                    const int mi = a.row_member[t];
+                    if (!vload(a.state[mi].refine)) continue;
+                    const Member &m = a.mem[mi];
+                    const double *xi = m.x[pass & 1];
+                    double *xo = m.x[1 - (pass & 1)];
+                    const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+                    for (int j = r0; j < r1; ++j)
+                        for (int i = lane; i < m.w; i += 32) {
+                            const size_t o = (size_t)j * m.ld + i;
+                            xo[o] = __fma_rn(ref_residual(xi, m.bx, m.ld, m.w, m.h, i, j), 0.125, __ldcg(xi + o));
+                        }
+                }
+                if (!grid_sync(a)) return;
+            }
+            // r = b - A x (an even pass count leaves x in x[0]), sum r^2 per task
+            for (int t = gw; t < a.nrow_tasks; t += nw) {
+                const int mi = a.row_member[t];
+                if (!vload(a.state[mi].refine)) continue;
+                const Member &m = a.mem[mi];
+                const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+                double acc = 0.0;
+                for (int j = r0; j < r1; ++j)
+                    for (int i = lane; i < m.w; i += 32) {
+                        const double q = ref_residual(m.x[0], m.bx, m.ld, m.w, m.h, i, j);
+                        m.b[(size_t)j * m.ld + i] = (float)q;
+                        acc = __fma_rn(q, q, acc);
+                    }
+                acc = warp_sum(acc);
+                if (lane == 0) a.row_part[t] = acc;
+            }
+            if (!grid_sync(a)) return;
+            for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+                volatile MemberState &ms = a.state[k];
+                if (ms.done || !ms.refine) continue;
+                const Member &m = a.mem[k];
+                double rr = 0.0;
+                for (int t = 0; t < m.nrow; ++t) rr += __ldcg(a.row_part + m.row_task0 + t);
+                const double bb = ms.bb;
+                const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
+                const bool full = s - ms.refine_start >= m.interval;
+                ms.rel = rel;
+                ms.refine = 0;
+                ms.refines = ms.refines + 1;
+                if (rel <= a.tol || s == a.cap || (full && !(rel < kStallGain * ms.last_rel))) {
+                    ms.done = 1;
+                    ms.sweeps = s;
+                    ms.capped = rel > a.tol && s == a.cap ? 1 : 0;
+                    ms.stalled = rel > a.tol && s != a.cap ? 1 : 0;
+                    atomicSub(a.active + check, 1);
+                } else {
+                    ms.zero_phase = phase;  // the next sweep phase starts the new correction from zero
+                    ms.refine_start = s;
+                    ms.last_rel = rel;
+                }
+            }
+            if (!grid_sync(a)) return;
+        }
         if (*(volatile int *)(a.active + check) == 0) break;
         ++check;
     }
@@ -237,13 +416,20 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
     for (int t = gw; t < a.nrow_tasks; t += nw) {
         const int mi = a.row_member[t];
         const Member &m = a.mem[mi];
-        const float *pf = m.p[vload(a.state[mi].cur)];
         const size_t plane = (size_t)m.ld * m.h;
         const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
-        for (int j = r0; j < r1; ++j)
-            for (int i = lane; i < m.w; i += 32)
-                project_image_cell(m.u[1], m.v[1], pf, m.u[0], m.v[0], m.ld, m.w, m.h, a.dt, m.img[ic], m.img[io],
-                                   plane, a.channels, i, j);
+        if (REF) {
+            for (int j = r0; j < r1; ++j)
+                for (int i = lane; i < m.w; i += 32)
+                    ref_project_image_cell(m.u[1], m.v[1], m.x[0], m.u[0], m.v[0], m.p[0], m.ld, m.w, m.h, a.dt,
+                                           m.img[ic], m.img[io], plane, a.channels, i, j);
+        } else {
+            const float *pf = m.p[vload(a.state[mi].cur)];
+            for (int j = r0; j < r1; ++j)
+                for (int i = lane; i < m.w; i += 32)
+                    project_image_cell(m.u[1], m.v[1], pf, m.u[0], m.v[0], m.ld, m.w, m.h, a.dt, m.img[ic],
+                                       m.img[io], plane, a.channels, i, j);
+        }
     }
 }
 
@@ -281,6 +467,7 @@ struct Ensemble {
     bool graphs_ok = true;
     int *dsel = nullptr;  // member list of pfs_ensemble_image_stats (n ints)
     int stall_block = -1;  // test hook for the next step (pfs_ensemble_debug_stall_block)
+    bool refined = false;  // PFS_PREC_F32R members
 };
 
 namespace {
@@ -331,12 +518,12 @@ int build_tasks(Ensemble &E)
     return PFS_OK;
 }
 
-template <int G, int L>
+template <int G, int L, bool REF>
 cudaError_t launch_ens(const EnsArgs &a, int grid, cudaStream_t st)
 {
     constexpr int smem = Ring<float, L>::bytes_per_block;
     static std::atomic<unsigned long long> attr_done{0};  // per instantiation and device
-    const cudaError_t ea = smem_limit_once(k_ensemble_step<G, L>, smem, attr_done);
+    const cudaError_t ea = smem_limit_once(k_ensemble_step<G, L, REF>, smem, attr_done);
     if (ea != cudaSuccess) return ea;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
@@ -348,7 +535,7 @@ cudaError_t launch_ens(const EnsArgs &a, int grid, cudaStream_t st)
     attr_coop.val.cooperative = 1;
     cfg.attrs = &attr_coop;
     cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_ensemble_step<G, L>, a);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_ensemble_step<G, L, REF>, a);
     if (e == cudaSuccess) launched();
     return e;
 }
@@ -358,17 +545,16 @@ int grid_for(Ensemble &E)
     int dev, sms, per = 0;
     ECK(cudaGetDevice(&dev));
     ECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (E.levels == 8) {
-        cudaFuncSetAttribute(k_ensemble_step<8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             Ring<float, 8>::bytes_per_block);
-        ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble_step<8, 8>, 128,
-                                                          Ring<float, 8>::bytes_per_block));
-    } else {
-        cudaFuncSetAttribute(k_ensemble_step<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             Ring<float, 4>::bytes_per_block);
-        ECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ensemble_step<4, 4>, 128,
-                                                          Ring<float, 4>::bytes_per_block));
-    }
+    auto occ = [&](auto kernel, int smem) -> cudaError_t {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, smem);
+    };
+    if (E.levels == 8)
+        ECK(E.refined ? occ(k_ensemble_step<8, 8, true>, Ring<float, 8>::bytes_per_block)
+                      : occ(k_ensemble_step<8, 8, false>, Ring<float, 8>::bytes_per_block));
+    else
+        ECK(E.refined ? occ(k_ensemble_step<4, 4, true>, Ring<float, 4>::bytes_per_block)
+                      : occ(k_ensemble_step<4, 4, false>, Ring<float, 4>::bytes_per_block));
     if (per < 1) return ens_fail(PFS_ERR_UNSUPPORTED, "ensemble kernel does not fit on an SM");
     E.grid = per * sms;
     return PFS_OK;
@@ -392,6 +578,7 @@ EnsArgs make_args(Ensemble &E, int icur)
     a.bar_gen = E.dbar + 1;
     a.err = E.derr;
     a.active = E.dactive;
+    a.refining = E.dactive + E.prm.max_iters / 4 + 2;
     a.dt = E.prm.dt;
     a.gamma = (float)(-1.0 / (double)E.prm.dt);
     a.tol = E.prm.tol > 0.0 ? E.prm.tol : -1.0;
@@ -407,10 +594,13 @@ EnsArgs make_args(Ensemble &E, int icur)
 int enqueue_step(Ensemble &E, int icur, cudaStream_t st)
 {
     const int nchecks = E.prm.max_iters / E.levels + 2;
-    ECK(cudaMemsetAsync(E.dactive, 0, sizeof(int) * nchecks, st));
-    ECK(cudaMemsetAsync(E.dbar, 0, sizeof(unsigned) * 2, st));
     const EnsArgs a = make_args(E, icur);
-    const cudaError_t e = E.levels == 8 ? launch_ens<8, 8>(a, E.grid, st) : launch_ens<4, 4>(a, E.grid, st);
+    ECK(cudaMemsetAsync(a.active, 0, sizeof(int) * nchecks, st));
+    if (E.refined) ECK(cudaMemsetAsync(a.refining, 0, sizeof(int) * nchecks, st));
+    ECK(cudaMemsetAsync(E.dbar, 0, sizeof(unsigned) * 2, st));
+    cudaError_t e;
+    if (E.refined) e = E.levels == 8 ? launch_ens<8, 8, true>(a, E.grid, st) : launch_ens<4, 4, true>(a, E.grid, st);
+    else e = E.levels == 8 ? launch_ens<8, 8, false>(a, E.grid, st) : launch_ens<4, 4, false>(a, E.grid, st);
     ECK(e);
     return PFS_OK;
 }
@@ -473,9 +663,12 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
     *out = nullptr;
     const pfs_params &p = *params;
     if (!(p.dt > 0.0f) || p.viscosity != 0.0f || p.diffuse_iters < 2 || p.diffuse_iters % 2 ||
-        p.boundary != PFS_BOUNDARY_PERIODIC || p.precision != PFS_PREC_F32)
+        p.boundary != PFS_BOUNDARY_PERIODIC || (p.precision != PFS_PREC_F32 && p.precision != PFS_PREC_F32R))
         return pfs::record_error(PFS_ERR_UNSUPPORTED,
-                                 "ensembles run float32 steps with viscosity 0 and an even diffusion count >= 2");
+                                 "ensembles run float32 (F32 or F32R) steps with viscosity 0 and an even diffusion "
+                                 "count >= 2");
+    if (p.precision == PFS_PREC_F32R && !(p.tol > 0.0))
+        return pfs::record_error(PFS_ERR_UNSUPPORTED, "refined ensembles iterate to a tolerance (tol > 0)");
     const int L = p.fuse_depth > 0 ? p.fuse_depth : 8;
     if (L != 4 && L != 8) return pfs::record_error(PFS_ERR_UNSUPPORTED, "ensemble fuse_depth must be 4 or 8");
     if (p.max_iters <= 0 || p.max_iters % L || (p.check_every > 0 && p.check_every % L))
@@ -493,6 +686,9 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
     E->levels = L;
     E->halo = L == 8 ? 8 : 4;
     E->chunk = p.chunk_rows > 0 ? p.chunk_rows : 32;
+    E->refined = p.precision == PFS_PREC_F32R;
+    // per member: u, v x2, p x2, b, image x2 (c planes each); refined: x x2 (FP64, two floats per cell), bx
+    const int extra = E->refined ? 5 : 0;
     size_t tot = 0;
     E->hmem.resize(n);
     for (int k = 0; k < n; ++k) {
@@ -501,7 +697,7 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
         const int ld = (w[k] + 31) / 32 * 32;
         E->ld.push_back(ld);
         E->off.push_back(tot);
-        tot += (size_t)ld * h[k] * (7 + 2 * channels);
+        tot += (size_t)ld * h[k] * (7 + 2 * channels + extra);
     }
     E->floats = tot;
     int rc = PFS_OK;
@@ -527,13 +723,23 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
         m.b = q + 6 * P;
         m.img[0] = q + 7 * P;
         m.img[1] = q + (7 + channels) * P;
+        m.x[0] = m.x[1] = nullptr;
+        m.bx = nullptr;
+        m.interval = 0;
+        if (E->refined) {  // P is a multiple of 32 floats: the FP64 planes stay 8-byte aligned
+            float *r = q + (7 + 2 * channels) * P;
+            m.x[0] = reinterpret_cast<double *>(r);
+            m.x[1] = reinterpret_cast<double *>(r + 2 * P);
+            m.bx = r + 4 * P;
+            m.interval = pfs::f32r_refine_interval(std::max(m.w, m.h), p.check_every > 0 ? p.check_every : p.max_iters);
+        }
     }
     if (cudaMalloc(&E->dmem, sizeof(pfs::Member) * n) != cudaSuccess ||
         cudaMalloc(&E->dstate, sizeof(pfs::MemberState) * n) != cudaSuccess ||
         cudaMemset(E->dstate, 0, sizeof(pfs::MemberState) * n) != cudaSuccess ||
         cudaMalloc(&E->dbar, 2 * sizeof(unsigned)) != cudaSuccess ||
         cudaMalloc(&E->derr, sizeof(int)) != cudaSuccess || cudaMemset(E->derr, 0, sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&E->dactive, sizeof(int) * (p.max_iters / 4 + 2)) != cudaSuccess)  // any fuse depth (>= 4)
+        cudaMalloc(&E->dactive, 2 * sizeof(int) * (p.max_iters / 4 + 2)) != cudaSuccess)  // any fuse depth (>= 4)
         return bail(pfs::record_error(PFS_ERR_CUDA, "ensemble allocation failed"));
     if ((rc = pfs::build_tasks(*E)) != PFS_OK) return bail(rc);
     if ((rc = pfs::grid_for(*E)) != PFS_OK) return bail(rc);
@@ -692,6 +898,7 @@ int pfs_ensemble_upload(pfs_ensemble *e, int k, const float *vp, const float *tm
     }
     cudaError_t r = pfs::launch_split_velocity(A, m.u[0], m.v[0], m.ld, m.w, m.h, E->st);
     if (r == cudaSuccess) r = pfs::launch_split_channel(B, 2, 4, m.p[0], m.ld, m.w, m.h, E->st);
+    if (r == cudaSuccess && E->refined) r = pfs::launch_widen(m.p[0], m.x[0], (size_t)m.ld * m.h, E->st);
     if (r == cudaSuccess && E->c > 0)
         r = pfs::launch_split_image(I, m.img[E->icur], (size_t)m.ld * m.h, m.ld, m.w, m.h, E->c, E->st);
     pfs::MemberState ms{};
@@ -759,6 +966,7 @@ int pfs_ensemble_member_stats(pfs_ensemble *e, int k, pfs_stats *out)
     out->rel_residual = ms.rel;
     out->bnorm = std::sqrt(ms.bb);
     out->capped = ms.capped;
+    out->stalled = ms.stalled;
     out->steps = E->steps;
     return PFS_OK;
 }

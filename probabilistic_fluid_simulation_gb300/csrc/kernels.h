@@ -46,20 +46,65 @@ struct Reduce {
     int nblocks;
 };
 
-constexpr int kReduceBlocks = 608;  // 4 x 152 SMs
+// Capacity of the reduction scratch in blocks (partial-sum slots). The grids
+// of the reductions use reduce_grid(): four blocks per SM of the current
+// device, at most this many.
+constexpr int kReduceBlocks = 608;
+int reduce_grid();
+// Streaming multiprocessors of the current device (0 if it cannot be read).
+int device_sms();
 
 // Device-side state of one pressure solve in residual mode. The residual
-// kernel at a check point sets `done` when ||r||/||b|| <= tol; sweep and
-// residual launches enqueued after that see the flag and return at once.
+// kernel at a check point sets `done` when ||r||/||b|| <= tol, or, with a
+// stall window, when the relative residual has not fallen below 0.99 times
+// its best value for that many sweeps (the iterate has reached the rounding
+// floor of its storage); sweep and residual launches enqueued after that see
+// the flag and return at once.
 struct SolveState {
-    int done;
-    int sweeps;  // sweep count at the check that converged
-    int checks;  // residual evaluations performed
-    int pad;
-    double rel;  // last evaluated relative residual
-    double rr;   // last evaluated sum r^2
-    double bb;   // sum b^2 of this step's divergence
+    int done;         // 0 iterating, 1 converged, 2 stalled
+    int sweeps;       // sweep count at the check that set done
+    int checks;       // residual evaluations performed
+    int best_sweeps;  // sweep count at the check that last lowered `best`
+    double rel;       // last evaluated relative residual
+    double rr;        // last evaluated sum r^2
+    double bb;        // sum b^2 of this step's divergence
+    double best;      // smallest relative residual so far (0: none yet)
 };
+// A check lowers `best` when its residual is below this fraction of it.
+constexpr double kStallGain = 0.99;
+// Stall window in sweeps for a grid whose larger side is n, with checks every
+// `every` sweeps: long enough that the slowest mode of the exact iteration
+// (Jacobi eigenvalue (1 + cos(2 pi / n)) / 2 ~ 1 - pi^2 / n^2 on the periodic
+// grid) falls by 3% within it, so only rounding can stop the residual from
+// falling 1%, and at least two checks; a multiple of `every`.
+inline int auto_stall_window(int n, int every)
+{
+    const double w = 3.09e-3 * (double)n * (double)n;
+    const int e = every > 0 ? every : 1;
+    long long k = (long long)((w + e - 1) / e);
+    if (k < 2) k = 2;
+    if (k > (1 << 30) / e) k = (1 << 30) / e;
+    return (int)(k * e);
+}
+
+// Sweeps between refinements of the float32 refined form in residual mode
+// for a grid whose larger side is n. The float32 correction e can lower its
+// residual to about 4.5 * 2^-25 * rms(e) / rms(rt) of its right-hand side
+// (the rounding of e); once the residual is smooth, rms(e) / rms(rt) is about
+// n^2 / (4 pi^2), a floor of a few percent at 2048^2. In `interval` sweeps
+// the slowest mode of the iteration falls by exp(-interval * pi^2 / n^2),
+// 0.78 for interval = 0.025 n^2, so the correction is refined long before it
+// nears that floor, while the FP64 pass (one read of x, b and e, and the
+// damped passes) is rare: one per 105,000 sweeps at 2048^2. A multiple of the
+// check interval.
+inline int f32r_refine_interval(int n, int every)
+{
+    const double want = 0.025 * (double)n * (double)n;
+    long long k = (long long)((want + every - 1) / every);
+    if (k < 1) k = 1;
+    if (k > (1 << 30) / every) k = (1 << 30) / every;
+    return (int)(k * every);
+}
 
 // ---- velocity / image / layout (step_kernels.cu) ----
 cudaError_t launch_advect(const float *u, const float *v, float *uo, float *vo, int ld, int w, int h, float dt,
@@ -114,6 +159,9 @@ cudaError_t launch_zero_small(void *dst, size_t bytes, cudaStream_t st);
 
 // ---- pressure (sweep_kernels.cu, residual_kernels.cu) ----
 int stream_strip_width(int halo);
+// Rows per warp task of the fused sweep when the caller sets none (see
+// sweep_kernels.cu).
+int default_chunk(int w, int h, int levels);
 // `done` (may be null): skip the launch when *done != 0
 cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, int ld, int w, int h,
                                 const int *done, cudaStream_t st);
@@ -127,7 +175,8 @@ cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, f
 int sweep_stream_blocks(int w, int h, int chunk);
 cudaError_t launch_sweep_stream_check(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
                                       int h, int levels, int chunk, const Reduce &red, SolveState *state,
-                                      int sweeps_here, double tol, const int *done, cudaStream_t st);
+                                      int sweeps_here, double tol, const int *done, cudaStream_t st,
+                                      int stall_window = 0);
 // 16-bit storage, FP32 compute; pin == null means a zero input iterate. levels in [1, 8].
 cudaError_t launch_sweep_stream_bf16(const __nv_bfloat16 *pin, const __nv_bfloat16 *b, __nv_bfloat16 *pout, int ld,
                                      int w, int h, int levels, int chunk, cudaStream_t st);
@@ -138,7 +187,7 @@ cudaError_t launch_sweep_stream_f16(const __half *pin, const __half *b, __half *
 // check (rel = sqrt(r^2)/sqrt(b^2) from red.result[1]) and marks the solve
 // done at `sweeps_here` sweeps when rel <= tol.
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
-                            SolveState *state, int sweeps_here, double tol, cudaStream_t st);
+                            SolveState *state, int sweeps_here, double tol, cudaStream_t st, int stall_window = 0);
 // both sums in one pass: r^2 into red.result[0], b^2 into red.result[1]
 cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, const Reduce &red, cudaStream_t st);
 

@@ -99,7 +99,7 @@ extern "C" int pfs_residual_norms_static(const float *p, const float *b, int vx,
     red.partials = reinterpret_cast<double *>(scratch);
     red.result = reinterpret_cast<double *>(scratch + kResultOffset);
     red.ticket = reinterpret_cast<unsigned *>(scratch + kTicketOffset);
-    red.nblocks = pfs::kReduceBlocks;
+    red.nblocks = pfs::reduce_grid();
     cudaStream_t st = (cudaStream_t)stream;
     double out[2];
     cudaError_t e = cudaMemsetAsync(red.ticket, 0, 2 * sizeof(unsigned), st);

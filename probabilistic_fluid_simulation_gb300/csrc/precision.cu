@@ -244,6 +244,26 @@ __global__ void k_lp_scale(const float *__restrict__ r, T *__restrict__ rt, size
         rt[k] = Store<T>::from_f(r[k] * s);
 }
 
+// The float32 form's right-hand side: rt = r / max|r| over the grid's cells
+// (padding columns get 0) and sum rt^2 into red.result[1], the norm the fused
+// residual checks of the correction solve divide by.
+__global__ void __launch_bounds__(256) k_lp_scale_f32(const float *__restrict__ r, float *__restrict__ rt, int ld,
+                                                      int w, int h, const unsigned *maxabs, double *escale, Reduce red)
+{
+    const float m = __uint_as_float(*maxabs);
+    const float s = m > 0.0f ? 1.0f / m : 1.0f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *escale = (double)s;
+    FFAcc acc;
+    for (int j = blockIdx.x; j < h; j += gridDim.x)
+        for (int i = threadIdx.x; i < ld; i += blockDim.x) {
+            const size_t k = (size_t)j * ld + i;
+            const float v = i < w ? r[k] * s : 0.0f;
+            rt[k] = v;
+            acc_square(acc, v);
+        }
+    reduce_blocks(acc.value(), red, 1);
+}
+
 // FP64 form: one Jacobi sweep (src/fluid.cpp:239-257 in double). The
 // division by 4 is a multiplication by 0.25: both are the correctly rounded
 // value of the same exact quotient (4 is a power of two), so the bits are
@@ -404,6 +424,13 @@ struct LpState {
     Reduce red{};
     void *stage = nullptr;
     size_t stage_bytes = 0;
+    // F32R: the correction solve's fused residual checks (their own partials and
+    // result pair: result[1] holds sum rt^2) and its device / mapped solve state
+    Reduce red_in{};
+    double *in_mem = nullptr;
+    SolveState *dstate = nullptr;
+    SolveState *hstate = nullptr;  // pinned and mapped
+    SolveState *hstate_d = nullptr;
 };
 
 namespace {
@@ -475,7 +502,7 @@ int lp_network_start(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
         if (pass == 0) {
             LCK(launch_widen(s.pred, s.x[s.xcur], s.plane, st));
         } else {
-            k_lp_add<<<kReduceBlocks, 256, 0, st>>>(s.x[s.xcur], s.pred, s.plane);
+            k_lp_add<<<reduce_grid(), 256, 0, st>>>(s.x[s.xcur], s.pred, s.plane);
             LCK(launched());
         }
         for (int k = 0; k < PFS_START_DAMP_PASSES; ++k) {
@@ -512,6 +539,78 @@ cudaError_t lp_sweeps(const T *in, const T *rhs, T *out, int ld, int w, int h, i
         return launch_sweep_stream(in, rhs, out, nullptr, ld, w, h, L, 8, chunk, nullptr, st);
 }
 
+// Correction solve of the float32 refined form in residual mode: Jacobi
+// sweeps on A e = rt from e = 0 with the plain form's fused sweep kernel, the
+// last launch of every `every` sweeps evaluating the correction's exact
+// residual ||rt - A e|| / ||rt|| on the device (as the plain form's solve
+// does), until it is at most tol_in, or (window > 0) it has not fallen 1%
+// within `window` sweeps, or `budget` sweeps have run. The host reads the state between batches of check
+// intervals (1, 2, 4, ... 64); launches after the deciding check return at
+// once. Returns the sweeps done, the plane holding e and the state's done
+// code (0: budget spent, 1: converged, 2: stalled).
+int lp_correction_f32(LpState &s, const LpParams &p, double tol_in, int budget, int window, cudaStream_t st,
+                      int &sweeps, const float *&eout, int &done_code)
+{
+    const int every = p.check_every > 0 ? p.check_every : 32;
+    const int L = std::max(1, std::min(p.levels, 8));
+    const int chunk = std::max(p.chunk, 16);
+    const float *rt = (const float *)s.rt;
+    float *e[2] = {(float *)s.e[0], (float *)s.e[1]};
+    LCK(launch_zero_small(s.dstate, sizeof(SolveState), st));
+    const int *done = &s.dstate->done;
+    struct Mark {
+        int sweeps, plane;
+    };
+    Mark marks[64];
+    int nmarks = 0, S = 0, cur = -1, batch = 1, in_batch = 0;
+    bool finished = budget <= 0;
+    while (!finished) {
+        const int stop = std::min(budget, (S / every + 1) * every);
+        while (S < stop) {
+            int n = std::min(L, stop - S);
+            bool last = (S + n == stop);
+            if (last && n == 8) {  // the check launch fuses at most 7 levels: 8 = 4 + 4
+                n = 4;
+                last = false;
+            }
+            const int out = cur == 0 ? 1 : 0;
+            const float *in = cur < 0 ? nullptr : e[cur];  // null: the zero start
+            if (last)
+                LCK(launch_sweep_stream_check(in, rt, e[out], nullptr, s.ld, s.w, s.h, n, chunk, s.red_in, s.dstate,
+                                              S + n, tol_in, done, st, window));
+            else
+                LCK(launch_sweep_stream(in, rt, e[out], nullptr, s.ld, s.w, s.h, n, 8, chunk, done, st));
+            cur = out;
+            S += n;
+        }
+        marks[nmarks++] = {S, cur};
+        if (++in_batch == batch || S >= budget || nmarks == 64) {
+            LCK(launch_copy_small(s.dstate, s.hstate_d, sizeof(SolveState), st));
+            LCK(cudaStreamSynchronize(st));
+            if (s.hstate->done || S >= budget) {
+                finished = true;
+            } else {
+                nmarks = 0;  // the deciding check can only be in a later batch
+                in_batch = 0;
+                batch = std::min(batch * 2, 64);
+            }
+        }
+    }
+    const SolveState hs = *s.hstate;
+    done_code = hs.done;
+    int plane = cur;
+    if (hs.done) {
+        int k = nmarks - 1;
+        while (k > 0 && marks[k].sweeps != hs.sweeps) --k;
+        if (nmarks == 0 || marks[k].sweeps != hs.sweeps) return lp_fail(PFS_ERR_CUDA, "lost the deciding check");
+        S = hs.sweeps;
+        plane = marks[k].plane;
+    }
+    sweeps = S;
+    eout = (S > 0 && plane >= 0) ? e[plane] : nullptr;
+    return PFS_OK;
+}
+
 // One step of a refined form (bf16, fp16 or float32 storage).
 template <typename T>
 int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
@@ -538,7 +637,22 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
     double last_rel = o.rel_start;
     int S = 0;
     T *ecur = nullptr;  // correction of the last inner solve (null before the first)
+    bool stalled_in = false;  // the last correction solve ran its whole interval without converging
+    double best_rel = 0.0;    // lowest residual of the 16-bit forms' refinements so far
+    int best_sweeps = 0;
     o.checks = 0;
+    // The float32 form in residual mode filters each correction before the
+    // residual: the Jacobi iteration multiplies the checkerboard mode of an
+    // error by -1 every sweep and the modes near it by almost -1, so the
+    // rounding noise that a float32 correction picks up in them over its
+    // thousands of sweeps is never damped by later sweeps (in exact arithmetic
+    // neither b nor the iterates carry these modes: the central-difference
+    // divergence has no checkerboard component). At 2048^2 that noise held the
+    // residual near 2.6e-5. PFS_START_DAMP_PASSES damped passes x += (b - A x) / 8
+    // in FP64 after x += e remove it (gain (1 + mu) / 2 on a mode of Jacobi
+    // eigenvalue mu: 0 on the checkerboard, about 1 on the smooth modes the
+    // iteration is working on).
+    const bool filter = std::is_same<T, float>::value && resid;
     for (;;) {
         // x_new = x + e/scale; r = b - A x_new (FP64); |r| stats
         LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
@@ -546,6 +660,21 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
                                                        s.x[1 - s.xcur], s.r, ld, w, h, s.red, s.maxabs);
         LCK(launched());
         s.xcur = 1 - s.xcur;
+        if (filter && ecur) {
+            for (int k = 0; k < PFS_START_DAMP_PASSES; ++k) {
+                k_lp_damp<<<g2(w, h), dim3(kBX, kBY), 0, st>>>(s.x[s.xcur], (const float *)s.b, s.x[1 - s.xcur], ld,
+                                                               w, h);
+                LCK(launched());
+                s.xcur = 1 - s.xcur;
+            }
+            // the residual of the filtered pressure (no correction: x is copied through)
+            LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
+            k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], (const T *)nullptr, s.escale,
+                                                           (const float *)s.b, s.x[1 - s.xcur], s.r, ld, w, h, s.red,
+                                                           s.maxabs);
+            LCK(launched());
+            s.xcur = 1 - s.xcur;
+        }
         LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
         LCK(cudaStreamSynchronize(st));
         o.checks++;
@@ -558,7 +687,45 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
             ecur = nullptr;  // next pass: residual of the previous pressure, no correction
             continue;
         }
+        if constexpr (std::is_same<T, float>::value) {
+            if (resid) {
+                // a correction solve that ran its whole interval must have bought a 1% fall
+                if (stalled_in && !(o.rel < kStallGain * last_rel)) {
+                    o.stalled = true;
+                    break;
+                }
+                last_rel = o.rel;
+                const double rn = std::sqrt(s.hres[0]), bn = std::sqrt(s.hres[1]);
+                // the correction's residual relative to its own right-hand side that
+                // makes the pressure's relative residual tol (the scaled float32
+                // right-hand side carries r to a relative 2^-24)
+                const double tol_in = rn > 0.0 ? 0.999 * p.tol * bn / rn : 0.0;
+                k_lp_scale_f32<<<reduce_grid(), 256, 0, st>>>(s.r, (float *)s.rt, ld, w, h, s.maxabs, s.escale,
+                                                               s.red_in);
+                LCK(launched());
+                const int every = p.check_every > 0 ? p.check_every : 32;
+                const int interval = f32r_refine_interval(std::max(w, h), every);
+                int n = 0, code = 0;
+                const float *eo = nullptr;
+                const int rc = lp_correction_f32(s, p, tol_in, std::min(interval, p.max_iters - S), 0, st, n, eo, code);
+                if (rc != PFS_OK) return rc;
+                stalled_in = code == 0 && n == interval;
+                ecur = (T *)const_cast<float *>(eo);
+                S += n;
+                continue;
+            }
+        }
         last_rel = o.rel;
+        // the 16-bit forms: stop once the refinements stop lowering the residual (their rounding floor)
+        if (resid && p.stall_window > 0) {
+            if (best_rel == 0.0 || o.rel < kStallGain * best_rel) {
+                best_rel = o.rel;
+                best_sweeps = S;
+            } else if (S - best_sweeps >= p.stall_window) {
+                o.stalled = true;
+                break;
+            }
+        }
         // inner solve: n sweeps on A e = r from e = 0
         const int n = std::min(m, p.max_iters - S);
         k_lp_scale<T><<<s.red.nblocks, 256, 0, st>>>(s.r, (T *)s.rt, s.plane, s.maxabs, s.escale);
@@ -576,7 +743,7 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
         S += n;
     }
     o.sweeps = S;
-    o.capped = p.tol > 0.0 && !(o.rel <= p.tol);
+    o.capped = p.tol > 0.0 && !(o.rel <= p.tol) && !o.stalled;
     return lp_velocity_and_image<T, float>(s, p, st, s.x[s.xcur]);
 }
 
@@ -723,8 +890,28 @@ int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
     s->red.result = s->rmem + 2 * nb;
     s->escale = s->rmem + 2 * nb + 2;
     s->red.ticket = reinterpret_cast<unsigned *>(s->rmem + 2 * nb + 3);
-    s->red.nblocks = nb;
+    s->red.nblocks = reduce_grid();
     s->maxabs = s->red.ticket + 2;
+    if (form == PFS_PREC_F32R) {
+        // the correction solve's checks: partials for the fused check launches at chunks of 16 rows or
+        // more and for the scale kernel's norm | result pair | two tickets
+        const int ns = std::max(reduce_grid(), sweep_stream_blocks(w, h, 16));
+        const size_t ibytes = (2 * (size_t)ns + 2) * sizeof(double) + 16;
+        e = cudaMalloc(&s->in_mem, ibytes);
+        if (e == cudaSuccess) e = cudaMemset(s->in_mem, 0, ibytes);
+        if (e == cudaSuccess) e = cudaMalloc(&s->dstate, sizeof(SolveState));
+        if (e == cudaSuccess) e = cudaMemset(s->dstate, 0, sizeof(SolveState));
+        if (e == cudaSuccess) e = cudaHostAlloc(&s->hstate, sizeof(SolveState), cudaHostAllocMapped);
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)&s->hstate_d, s->hstate, 0);
+        if (e != cudaSuccess) {
+            lp_destroy(s);
+            return lp_fail(PFS_ERR_CUDA, cudaGetErrorString(e));
+        }
+        s->red_in.partials = s->in_mem;
+        s->red_in.result = s->in_mem + 2 * (size_t)ns;
+        s->red_in.ticket = reinterpret_cast<unsigned *>(s->in_mem + 2 * (size_t)ns + 2);
+        s->red_in.nblocks = ns;
+    }
     *out = s;
     return PFS_OK;
 }
@@ -738,6 +925,9 @@ void lp_destroy(LpState *s)
     if (s->stage) cudaFree(s->stage);
     if (s->xback) cudaFree(s->xback);
     if (s->pred) cudaFree(s->pred);
+    if (s->in_mem) cudaFree(s->in_mem);
+    if (s->dstate) cudaFree(s->dstate);
+    if (s->hstate) cudaFreeHost(s->hstate);
     delete s;
 }
 

@@ -24,6 +24,7 @@ struct LpParams {
     unet::Net *net = nullptr;             // the network of a PFS_START_NETWORK start
     int coarsen = 1;                      // network run on the grid coarsened this many times
     int passes = 1;                       // network applications (later ones on the residual)
+    int stall_window = 0;                 // residual mode: sweeps without a 1% fall that end the solve
 };
 
 struct LpOut {
@@ -33,6 +34,7 @@ struct LpOut {
     int start_kind = PFS_START_PREVIOUS;
     double rel_start = -1.0;
     int start_passes = 0;
+    bool stalled = false;
 };
 
 int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic);

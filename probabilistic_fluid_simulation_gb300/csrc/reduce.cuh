@@ -14,7 +14,7 @@ namespace {
 // kernel do not mix their counts). The order of additions is fixed, so the sum is
 // reproducible run to run.
 __device__ void reduce_blocks(double acc, const Reduce &red, int slot, SolveState *state = nullptr,
-                              int sweeps_here = 0, double tol = 0.0)
+                              int sweeps_here = 0, double tol = 0.0, int stall_window = 0)
 {
     __shared__ double ws[32];
     __shared__ bool last;
@@ -65,6 +65,14 @@ __device__ void reduce_blocks(double acc, const Reduce &red, int slot, SolveStat
                 if (rel <= tol) {
                     state->sweeps = sweeps_here;
                     state->done = 1;
+                } else if (stall_window > 0) {
+                    if (state->best == 0.0 || rel < kStallGain * state->best) {
+                        state->best = rel;
+                        state->best_sweeps = sweeps_here;
+                    } else if (sweeps_here - state->best_sweeps >= stall_window) {
+                        state->sweeps = sweeps_here;
+                        state->done = 2;
+                    }
                 }
             }
         }

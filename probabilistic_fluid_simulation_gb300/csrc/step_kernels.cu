@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) k_divergence(const float *__restrict__ u,
 
 __global__ void __launch_bounds__(256) k_residual(const float *__restrict__ p, const float *__restrict__ b, int ld,
                                                   int w, int h, Reduce red, SolveState *state, int sweeps_here,
-                                                  double tol)
+                                                  double tol, int stall_window)
 {
     if (state && *(volatile int *)&state->done) return;  // same answer for every block
     FFAcc acc;
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) k_residual(const float *__restrict__ p, c
         for (int i = threadIdx.x; i < w; i += blockDim.x)
             residual_sq(acc, b[r + i], p[r + wm(i, w)], p[r + wp(i, w)], p[rm + i], p[rp + i], p[r + i]);
     }
-    reduce_blocks(acc.value(), red, 0, state, sweeps_here, tol);
+    reduce_blocks(acc.value(), red, 0, state, sweeps_here, tol, stall_window);
 }
 
 __global__ void __launch_bounds__(256) k_norms(const float *__restrict__ p, const float *__restrict__ b, int ld, int w,
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *
                                                                    const float *__restrict__ b, int ld, int w,
                                                                    int h, int nsx, int nwork, Reduce red,
                                                                    SolveState *state, int sweeps_here, double tol,
-                                                                   int with_b)
+                                                                   int with_b, int stall_window)
 {
     if (state && *(volatile int *)&state->done) return;  // same answer for every block
     const int lane = threadIdx.x & 31;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kResWarps * 32) k_residual_strip(const float *
         const int y0 = sy * kResChunk, y1 = min(h, y0 + kResChunk);
         residual_strip_task(p, b, ld, w, h, sx, y0, y1, lane, acc, with_b ? &accb : nullptr);
     }
-    reduce_blocks(acc[0].value() + acc[1].value(), red, 0, state, sweeps_here, tol);
+    reduce_blocks(acc[0].value() + acc[1].value(), red, 0, state, sweeps_here, tol, stall_window);
     if (with_b) {
         __syncthreads();
         reduce_blocks(accb.value(), red, 1);
@@ -247,7 +247,7 @@ __global__ void k_widen(const float *__restrict__ in, double *__restrict__ out, 
 cudaError_t launch_widen(const float *in, double *out, size_t n, cudaStream_t st)
 {
     if (!out || !n) return cudaSuccess;
-    k_widen<<<kReduceBlocks, 256, 0, st>>>(in, out, n);
+    k_widen<<<reduce_grid(), 256, 0, st>>>(in, out, n);
     return launched();
 }
 
@@ -301,7 +301,7 @@ __global__ void k_add(float *__restrict__ p, const float *__restrict__ d, size_t
 
 cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
 {
-    k_add<<<kReduceBlocks, 256, 0, st>>>(p, d, n);
+    k_add<<<reduce_grid(), 256, 0, st>>>(p, d, n);
     return launched();
 }
 
@@ -357,7 +357,33 @@ cudaError_t launch_divergence(const float *u, const float *v, float *b, int ld, 
     return launched();
 }
 
-static bool strip_ok(int w, int ld) { return w % 4 == 0 && ld % 4 == 0; }
+int device_sms()
+{
+    static std::atomic<int> cached[64];  // per device ordinal, 0 = not yet read
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    int n = cached[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 0;
+        cached[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
+int reduce_grid()
+{
+    const int sms = device_sms();
+    return sms > 0 ? std::min(kReduceBlocks, 4 * sms) : kReduceBlocks;
+}
+
+// The strip kernel loads four cells of p and b at once (16-byte vector loads),
+// so it needs w and ld multiples of 4 and both planes 16-byte aligned; any
+// other layout (an offset view of a caller's plane, for one) takes the scalar
+// kernel, which gives the same sums.
+static bool strip_ok(const float *p, const float *b, int w, int ld)
+{
+    return w % 4 == 0 && ld % 4 == 0 && (((uintptr_t)p | (uintptr_t)b) & 15u) == 0;
+}
 
 static void strip_grid(int w, int h, int nblocks_max, int &nsx, int &nwork, int &blocks)
 {
@@ -367,24 +393,25 @@ static void strip_grid(int w, int h, int nblocks_max, int &nsx, int &nwork, int 
 }
 
 cudaError_t launch_residual(const float *p, const float *b, int ld, int w, int h, const Reduce &red,
-                            SolveState *state, int sweeps_here, double tol, cudaStream_t st)
+                            SolveState *state, int sweeps_here, double tol, cudaStream_t st, int stall_window)
 {
-    if (strip_ok(w, ld)) {
+    if (strip_ok(p, b, w, ld)) {
         int nsx, nwork, blocks;
         strip_grid(w, h, red.nblocks, nsx, nwork, blocks);
-        k_residual_strip<<<blocks, kResWarps * 32, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, state, sweeps_here, tol, 0);
+        k_residual_strip<<<blocks, kResWarps * 32, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, state, sweeps_here, tol, 0,
+                                                             stall_window);
         return launched();
     }
-    k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red, state, sweeps_here, tol);
+    k_residual<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red, state, sweeps_here, tol, stall_window);
     return launched();
 }
 
 cudaError_t launch_norms(const float *p, const float *b, int ld, int w, int h, const Reduce &red, cudaStream_t st)
 {
-    if (strip_ok(w, ld)) {
+    if (strip_ok(p, b, w, ld)) {
         int nsx, nwork, blocks;
         strip_grid(w, h, red.nblocks, nsx, nwork, blocks);
-        k_residual_strip<<<blocks, kResWarps * 32, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, nullptr, 0, 0.0, 1);
+        k_residual_strip<<<blocks, kResWarps * 32, 0, st>>>(p, b, ld, w, h, nsx, nwork, red, nullptr, 0, 0.0, 1, 0);
         return launched();
     }
     k_norms<<<red.nblocks, 256, 0, st>>>(p, b, ld, w, h, red);

@@ -17,13 +17,15 @@ int sweep_stream_blocks(int w, int h, int chunk)
 
 cudaError_t launch_sweep_stream_check(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,
                                       int h, int levels, int chunk, const Reduce &red, SolveState *state,
-                                      int sweeps_here, double tol, const int *done, cudaStream_t st)
+                                      int sweeps_here, double tol, const int *done, cudaStream_t st,
+                                      int stall_window)
 {
     StreamArgs<float> a = stream_args(pin, b, pout, pprev, ld, w, h, 8, chunk, done);
     a.red = red;
     a.state = state;
     a.sweeps_here = sweeps_here;
     a.tol = tol;
+    a.stall_window = stall_window;
     const bool prev = pprev != nullptr;
     switch (levels) {
     case 1: return prev ? launch_stream_t<float, 8, 1, true, true>(a, st) : launch_stream_t<float, 8, 1, false, true>(a, st);

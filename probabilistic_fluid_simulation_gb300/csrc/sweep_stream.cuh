@@ -52,6 +52,7 @@ struct StreamArgs {
     SolveState *state;   // records the check, raises done at or below tol
     int sweeps_here;     // sweep count of the solve after this launch
     double tol;
+    int stall_window;    // > 0: stop when the residual stops falling (SolveState)
 };
 
 // Rows in flight per warp (cp.async prefetch depth).

@@ -52,7 +52,8 @@ class Params(C.Structure):
     """pfs_params (include/pfs.h)."""
     _fields_ = [("dt", C.c_float), ("viscosity", C.c_float), ("diffuse_iters", C.c_int), ("max_iters", C.c_int),
                 ("tol", C.c_double), ("check_every", C.c_int), ("fuse_depth", C.c_int), ("chunk_rows", C.c_int),
-                ("want_residual", C.c_int), ("precision", C.c_int), ("boundary", C.c_int)]
+                ("want_residual", C.c_int), ("precision", C.c_int), ("boundary", C.c_int),
+                ("stall_sweeps", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -60,7 +61,7 @@ class Stats(C.Structure):
     _fields_ = [("sweeps", C.c_int), ("checks", C.c_int), ("rel_residual", C.c_double), ("bnorm", C.c_double),
                 ("capped", C.c_int), ("steps", C.c_longlong), ("total_sweeps", C.c_longlong),
                 ("cap_hits", C.c_longlong), ("start_kind", C.c_int), ("rel_start", C.c_double),
-                ("start_passes", C.c_int)]
+                ("start_passes", C.c_int), ("stalled", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -92,7 +92,7 @@ def main():
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--levels", type=int, default=8)
-    ap.add_argument("--chunk", type=int, default=32)
+    ap.add_argument("--chunk", type=int, default=0, help="rows per warp task; 0: the library default for the grid")
     ap.add_argument("--reps", type=int, default=100)
     ap.add_argument("--scan", action="store_true")
     ap.add_argument("--scan-levels", default=",".join(str(x) for x in LEVELS), help="fuse depths for --scan")

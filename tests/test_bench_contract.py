@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_line():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--size", "128",
-                        "--steps", "1", "--warmup", "0", "--ref-budget-s", "1"],
+                        "--steps", "2", "--warmup", "1", "--cpu-sample-sweeps", "20"],
                        capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -22,8 +22,10 @@ def test_reference_arm_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["unit"] == "cell-updates/s" and d["dtype"] == "f32"
     assert "workload" in d["config"]
+    assert d["steps"] == 2 and d["warmup"] == 1  # the steps and warm-up it was asked for
     cb = d["cpu_baseline"]
-    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] == 1 and cb["value"] == d["value"] and cb["sample"]
+    assert cb["all_cores_not_the_reference"]["value"] > 0
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0

@@ -154,3 +154,77 @@ def test_grid_barrier_timeout_is_reported(cuda_device, pfs_lib):
         ens.download(1, a, c)
     ref = session_run(pfs_lib, *states[1], 2, **kw)
     assert np.array_equal(a[..., :2], ref[0][..., :2]) and np.array_equal(c, ref[2])
+
+
+def test_ensemble_64_members_up_to_1024_equal_sessions(cuda_device, pfs_lib):
+    """64 members with sides drawn from {64, 128, 256, 512, 1024} (w and h
+    independently, as the ensemble workload draws them), residual stop, the
+    default tile: every member bit-equal to a plain session."""
+    rng = np.random.default_rng(2024)
+    sides = (64, 128, 256, 512, 1024)
+    sizes = [(int(sides[rng.integers(5)]), int(sides[rng.integers(5)])) for _ in range(64)]
+    assert max(max(s) for s in sizes) == 1024
+    kw = dict(dt=0.05, diffuse_iters=2, max_iters=400, tol=2e-2, check_every=40)
+    states = [member_state(w, h, k) for k, (w, h) in enumerate(sizes)]
+    with pfs_lib.Ensemble(sizes, 3, **kw) as ens:
+        for k, (vp, tmp, img) in enumerate(states):
+            ens.upload(k, vp, tmp, img)
+        ens.step(2)
+        stats = [ens.stats(k) for k in range(len(sizes))]
+        outs = []
+        for k, (vp, tmp, img) in enumerate(states):
+            a, c = np.empty_like(vp), np.empty_like(img)
+            ens.download(k, a, c)
+            outs.append((a, c))
+    for k, (vp, tmp, img) in enumerate(states):
+        sa, sb, sc, sst = session_run(pfs_lib, vp, tmp, img, 2, **kw)
+        a, c = outs[k]
+        assert np.array_equal(a[..., 0:2], sa[..., 0:2]), (k, sizes[k])
+        assert np.array_equal(a[..., 2], sb[..., 2]), (k, sizes[k])
+        assert np.array_equal(c, sc), (k, sizes[k])
+        assert stats[k]["sweeps"] == sst[-1]["sweeps"], (k, stats[k], sst[-1])
+    assert len({s["sweeps"] for s in stats}) >= 2  # members stop at different check points
+
+
+def test_refined_ensemble_members_match_refined_sessions(cuda_device, pfs_lib):
+    """PFS_PREC_F32R members (float32 sweeps on a correction, FP64 pressure and
+    refinement) reach the tolerance the float32 form cannot, and match
+    PFS_PREC_F32R sessions: the same sweeps per step (the same check points,
+    refinement intervals and decisions), and fields within 1e-5 of the
+    session's (the ensemble does not scale the correction's right-hand side,
+    so its float32 rounding differs)."""
+    sizes = [(64, 64), (128, 64), (64, 128), (128, 128), (96, 40), (256, 128)]
+    kw = dict(dt=0.1, diffuse_iters=2, max_iters=200_000, tol=1e-5, check_every=200, precision=pfs_lib.PREC_F32R)
+    states = [member_state(w, h, k) for k, (w, h) in enumerate(sizes)]
+    steps = 2
+    with pfs_lib.Ensemble(sizes, 3, **kw) as ens:
+        for k, (vp, tmp, img) in enumerate(states):
+            ens.upload(k, vp, tmp, img)
+        per_step = []
+        for _ in range(steps):
+            ens.step(1)
+            per_step.append([ens.stats(k) for k in range(len(sizes))])
+        outs = []
+        for k, (vp, tmp, img) in enumerate(states):
+            a, c = np.empty_like(vp), np.empty_like(img)
+            ens.download(k, a, c)
+            outs.append((a, c))
+    for k, (vp, tmp, img) in enumerate(states):
+        h, w, _ = vp.shape
+        with pfs_lib.Session(w, h, image_shape=img.shape, **kw) as s:
+            s.upload(vp, tmp, img)
+            sst = []
+            for _ in range(steps):
+                s.step(1)
+                sst.append(s.stats())
+            sa, sc = np.empty_like(vp), np.empty_like(img)
+            s.download(sa, None, sc)
+        a, c = outs[k]
+        for step in range(steps):
+            e, q = per_step[step][k], sst[step]
+            assert e["rel_residual"] <= 1e-5 and not e["capped"] and not e["stalled"], (k, step, e)
+            assert abs(e["sweeps"] - q["sweeps"]) <= 200, (k, step, e, q)
+        for ch in (0, 1):
+            d = np.abs(a[..., ch] - sa[..., ch]).max() / np.abs(sa[..., ch]).max()
+            assert d < 1e-5, (k, ch, d)
+        assert np.abs(c - sc).max() < 1e-5, k

@@ -6,6 +6,7 @@ here is exact equality (np.array_equal, which treats +0 and -0 as equal:
 with viscosity 0 the reference's identity diffusion sweeps can flip the
 sign of a zero, which the GPU path does not replay).
 """
+import ctypes
 import hashlib
 
 import numpy as np
@@ -292,6 +293,36 @@ def test_residual_norms_match_oracle(cuda_device, pfs_lib, oracle_mod):
     vp[..., 3] = rng.standard_normal((96, 128)).astype(np.float32)
     rel, bn = oracle_mod.residual(vp)
     rr, bb = pfs_lib.residual_norms(dev(vp[..., 2].copy()), dev(vp[..., 3].copy()))
+    assert np.sqrt(bb) == pytest.approx(bn, rel=1e-12)
+    assert np.sqrt(rr) / np.sqrt(bb) == pytest.approx(rel, rel=1e-12)
+
+
+@pytest.mark.parametrize("static", [False, True])
+def test_residual_norms_of_unaligned_views(cuda_device, pfs_lib, oracle_mod, static):
+    # Views that start one float into their planes (4-byte, not 16-byte
+    # aligned) with a width divisible by 4: the vector-load kernel must not be
+    # chosen for them (its 16-byte loads would be misaligned); the host picks
+    # the scalar kernel before any launch, and the norms are the oracle's.
+    import torch
+    w, h = 128, 40
+    rng = np.random.default_rng(11)
+    vp = np.zeros((h, w, 4), np.float32)
+    vp[..., 2] = rng.standard_normal((h, w)).astype(np.float32)
+    vp[..., 3] = rng.standard_normal((h, w)).astype(np.float32)
+    rel, bn = oracle_mod.residual(vp)
+    ld = 160
+    pbase = torch.zeros(h, ld, device="cuda")
+    bbase = torch.zeros(h, ld, device="cuda")
+    pbase[:, 1:w + 1] = torch.from_numpy(vp[..., 2]).cuda()
+    bbase[:, 1:w + 1] = torch.from_numpy(vp[..., 3]).cuda()
+    pv, bv = pbase.data_ptr() + 4, bbase.data_ptr() + 4  # column 1 of each plane, row pitch ld
+    assert pv % 16 == 4 and bv % 16 == 4
+    lib = pfs_lib.lib()
+    fn = lib.pfs_residual_norms_static if static else lib.pfs_residual_norms
+    rrc, bbc = ctypes.c_double(), ctypes.c_double()
+    st = fn(ctypes.c_void_p(pv), ctypes.c_void_p(bv), w, h, ld, ctypes.byref(rrc), ctypes.byref(bbc), None)
+    assert st == 0, lib.pfs_last_error()
+    rr, bb = rrc.value, bbc.value
     assert np.sqrt(bb) == pytest.approx(bn, rel=1e-12)
     assert np.sqrt(rr) / np.sqrt(bb) == pytest.approx(rel, rel=1e-12)
 

@@ -53,3 +53,24 @@ def test_static_norms_reject_oversized_grid(cuda_device, pfs_lib):
     st = lib.pfs_residual_norms_static(C.c_void_p(p.data_ptr()), C.c_void_p(b.data_ptr()), 65536, 32768, 65536,
                                        C.byref(rr), C.byref(bb), None)
     assert st == 1 and b"exceeds" in lib.pfs_last_error()
+
+
+@pytest.mark.gpu
+def test_static_norms_allocate_no_device_memory(cuda_device, pfs_lib):
+    # The entry point's whole contract: no device allocation. Warm up first on
+    # other grid sizes (the first launch of each kernel path loads the
+    # library's kernels, which the driver may place in device memory), then
+    # call it repeatedly at new sizes and compare the device's free memory.
+    import torch
+    lib = pfs_lib.lib()
+    for w, h in ((260, 36), (37, 29)):  # vector-load and scalar kernel paths
+        p, b = _fields(w, h, seed=7)
+        assert _call(lib.pfs_residual_norms_static, p, b, w)[0] == 0, lib.pfs_last_error()
+    fields = [(_fields(w, h, seed=w), w) for w, h in ((1024, 768), (93, 61))]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for (p, b), w in fields:
+        for _ in range(3):
+            assert _call(lib.pfs_residual_norms_static, p, b, w)[0] == 0, lib.pfs_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
