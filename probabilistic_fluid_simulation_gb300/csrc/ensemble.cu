@@ -43,7 +43,7 @@ struct Member {
     float *p[2];         // pressure ping-pong (the refined form: the float32 correction e)
     float *b;            // divergence (the refined form: the correction's right-hand side r = b - A x)
     float *img[2];       // image ping-pong, c planes of ld*h each
-    double *x[2];        // the refined form: FP64 pressure and its damped-pass partner (else null)
+    double *x;           // the refined form: FP64 pressure (else null)
     float *bx;           // the refined form: the divergence b (else null)
     int interval;        // the refined form: sweeps between refinements (f32r_refine_interval)
     int row_task0, nrow;     // row tasks (8 rows): advect, divergence, projection + image
@@ -176,9 +176,10 @@ __device__ __forceinline__ void ref_project_image_cell(const float *__restrict__
 // the sweeps iterate a float32 correction e on A e = r, r = b - A x, with the
 // pressure x in FP64; at check points a member whose estimate
 // ||r - A e|| / ||b|| is below the tolerance, or whose correction has run
-// `interval` sweeps, is refined: x += e, PFS_START_DAMP_PASSES damped FP64
-// passes (which remove the rounding noise in the modes Jacobi cannot damp),
-// then r = b - A x and the FP64 residual decides.
+// `interval` sweeps, is refined: the correction is filtered by
+// PFS_START_DAMP_PASSES damped passes e += (r - A e) / 8, which remove the
+// rounding noise it gathered in the modes Jacobi cannot damp (as the refined
+// session form does), then x += e, r = b - A x, and the FP64 residual decides.
 template <int G, int L, bool REF>
 __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
 {
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             double acc = 0.0;
             for (int j = r0; j < r1; ++j)
                 for (int i = lane; i < m.w; i += 32) {
-                    const double q = ref_residual(m.x[0], m.bx, m.ld, m.w, m.h, i, j);
+                    const double q = ref_residual(m.x, m.bx, m.ld, m.w, m.h, i, j);
                     m.b[(size_t)j * m.ld + i] = (float)q;
                     acc = __fma_rn(q, q, acc);
                 }
@@ -334,6 +335,30 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         }
         if (!grid_sync(a)) return;
         if (REF && *(volatile int *)(a.refining + check) > 0) {
+            // the filter: damped passes e += (r - A e) / 8 on the correction, through the other
+            // correction plane (an even count ends back in e's plane)
+            for (int pass = 0; pass < PFS_START_DAMP_PASSES; ++pass) {
+                for (int t = gw; t < a.nrow_tasks; t += nw) {
+                    const int mi = a.row_member[t];
+                    if (!vload(a.state[mi].refine)) continue;
+                    const Member &m = a.mem[mi];
+                    const int ep = (vload(a.state[mi].cur) + phase) & 1;
+                    const float *ei = m.p[(pass & 1) ? 1 - ep : ep];
+                    float *eo = m.p[(pass & 1) ? ep : 1 - ep];
+                    const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+                    for (int j = r0; j < r1; ++j)
+                        for (int i = lane; i < m.w; i += 32) {
+                            const size_t r = (size_t)j * m.ld;
+                            const float q = fsub(fadd(fadd(fadd(fadd(__ldcg(m.b + r + i), __ldcg(ei + r + wm(i, m.w))),
+                                                                __ldcg(ei + r + wp(i, m.w))),
+                                                           __ldcg(ei + (size_t)wm(j, m.h) * m.ld + i)),
+                                                      __ldcg(ei + (size_t)wp(j, m.h) * m.ld + i)),
+                                                 fmul(4.0f, __ldcg(ei + r + i)));
+                            eo[r + i] = fadd(__ldcg(ei + r + i), fmul(q, 0.125f));
+                        }
+                }
+                if (!grid_sync(a)) return;
+            }
             // x += e for the refining members
             for (int t = gw; t < a.nrow_tasks; t += nw) {
                 const int mi = a.row_member[t];
@@ -344,28 +369,11 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
                 for (int j = r0; j < r1; ++j)
                     for (int i = lane; i < m.w; i += 32) {
                         const size_t o = (size_t)j * m.ld + i;
-                        m.x[0][o] = __dadd_rn(__ldcg(m.x[0] + o), (double)__ldcg(e + o));
+                        m.x[o] = __dadd_rn(__ldcg(m.x + o), (double)__ldcg(e + o));
                     }
             }
             if (!grid_sync(a)) return;
-            // damped passes x += (b - A x) / 8, x[0] -> x[1] -> x[0] ...
-            for (int pass = 0; pass < PFS_START_DAMP_PASSES; ++pass) {
-                for (int t = gw; t < a.nrow_tasks; t += nw) {
-                    const int mi = a.row_member[t];
-                    if (!vload(a.state[mi].refine)) continue;
-                    const Member &m = a.mem[mi];
-                    const double *xi = m.x[pass & 1];
-                    double *xo = m.x[1 - (pass & 1)];
-                    const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
-                    for (int j = r0; j < r1; ++j)
-                        for (int i = lane; i < m.w; i += 32) {
-                            const size_t o = (size_t)j * m.ld + i;
-                            xo[o] = __fma_rn(ref_residual(xi, m.bx, m.ld, m.w, m.h, i, j), 0.125, __ldcg(xi + o));
-                        }
-                }
-                if (!grid_sync(a)) return;
-            }
-            // r = b - A x (an even pass count leaves x in x[0]), sum r^2 per task
+            // r = b - A x, sum r^2 per task
             for (int t = gw; t < a.nrow_tasks; t += nw) {
                 const int mi = a.row_member[t];
                 if (!vload(a.state[mi].refine)) continue;
@@ -374,7 +382,7 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
                 double acc = 0.0;
                 for (int j = r0; j < r1; ++j)
                     for (int i = lane; i < m.w; i += 32) {
-                        const double q = ref_residual(m.x[0], m.bx, m.ld, m.w, m.h, i, j);
+                        const double q = ref_residual(m.x, m.bx, m.ld, m.w, m.h, i, j);
                         m.b[(size_t)j * m.ld + i] = (float)q;
                         acc = __fma_rn(q, q, acc);
                     }
@@ -421,7 +429,7 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         if (REF) {
             for (int j = r0; j < r1; ++j)
                 for (int i = lane; i < m.w; i += 32)
-                    ref_project_image_cell(m.u[1], m.v[1], m.x[0], m.u[0], m.v[0], m.p[0], m.ld, m.w, m.h, a.dt,
+                    ref_project_image_cell(m.u[1], m.v[1], m.x, m.u[0], m.v[0], m.p[0], m.ld, m.w, m.h, a.dt,
                                            m.img[ic], m.img[io], plane, a.channels, i, j);
         } else {
             const float *pf = m.p[vload(a.state[mi].cur)];
@@ -687,8 +695,8 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
     E->halo = L == 8 ? 8 : 4;
     E->chunk = p.chunk_rows > 0 ? p.chunk_rows : 32;
     E->refined = p.precision == PFS_PREC_F32R;
-    // per member: u, v x2, p x2, b, image x2 (c planes each); refined: x x2 (FP64, two floats per cell), bx
-    const int extra = E->refined ? 5 : 0;
+    // per member: u, v x2, p x2, b, image x2 (c planes each); refined: x (FP64, two floats per cell), bx
+    const int extra = E->refined ? 3 : 0;
     size_t tot = 0;
     E->hmem.resize(n);
     for (int k = 0; k < n; ++k) {
@@ -723,14 +731,13 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
         m.b = q + 6 * P;
         m.img[0] = q + 7 * P;
         m.img[1] = q + (7 + channels) * P;
-        m.x[0] = m.x[1] = nullptr;
+        m.x = nullptr;
         m.bx = nullptr;
         m.interval = 0;
         if (E->refined) {  // P is a multiple of 32 floats: the FP64 planes stay 8-byte aligned
             float *r = q + (7 + 2 * channels) * P;
-            m.x[0] = reinterpret_cast<double *>(r);
-            m.x[1] = reinterpret_cast<double *>(r + 2 * P);
-            m.bx = r + 4 * P;
+            m.x = reinterpret_cast<double *>(r);
+            m.bx = r + 2 * P;
             m.interval = pfs::f32r_refine_interval(std::max(m.w, m.h), p.check_every > 0 ? p.check_every : p.max_iters);
         }
     }
@@ -898,7 +905,7 @@ int pfs_ensemble_upload(pfs_ensemble *e, int k, const float *vp, const float *tm
     }
     cudaError_t r = pfs::launch_split_velocity(A, m.u[0], m.v[0], m.ld, m.w, m.h, E->st);
     if (r == cudaSuccess) r = pfs::launch_split_channel(B, 2, 4, m.p[0], m.ld, m.w, m.h, E->st);
-    if (r == cudaSuccess && E->refined) r = pfs::launch_widen(m.p[0], m.x[0], (size_t)m.ld * m.h, E->st);
+    if (r == cudaSuccess && E->refined) r = pfs::launch_widen(m.p[0], m.x, (size_t)m.ld * m.h, E->st);
     if (r == cudaSuccess && E->c > 0)
         r = pfs::launch_split_image(I, m.img[E->icur], (size_t)m.ld * m.h, m.ld, m.w, m.h, E->c, E->st);
     pfs::MemberState ms{};

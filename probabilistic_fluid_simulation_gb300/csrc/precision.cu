@@ -641,18 +641,18 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
     double best_rel = 0.0;    // lowest residual of the 16-bit forms' refinements so far
     int best_sweeps = 0;
     o.checks = 0;
-    // The float32 form in residual mode filters each correction before the
-    // residual: the Jacobi iteration multiplies the checkerboard mode of an
-    // error by -1 every sweep and the modes near it by almost -1, so the
-    // rounding noise that a float32 correction picks up in them over its
-    // thousands of sweeps is never damped by later sweeps (in exact arithmetic
-    // neither b nor the iterates carry these modes: the central-difference
-    // divergence has no checkerboard component). At 2048^2 that noise held the
-    // residual near 2.6e-5. PFS_START_DAMP_PASSES damped passes x += (b - A x) / 8
-    // in FP64 after x += e remove it (gain (1 + mu) / 2 on a mode of Jacobi
+    // The float32 form in residual mode filters each correction before adding
+    // it: the Jacobi iteration multiplies the checkerboard mode of an error by
+    // -1 every sweep and the modes near it by almost -1, so the rounding noise
+    // a float32 correction picks up in them over its thousands of sweeps would
+    // never be damped by later sweeps (in exact arithmetic neither b nor the
+    // iterates carry these modes: the central-difference divergence has no
+    // checkerboard component). Unfiltered, that noise held the residual near
+    // 2.6e-5 at 2048^2. PFS_START_DAMP_PASSES damped passes e += (rt - A e) / 8
+    // on the correction remove it (gain (1 + mu) / 2 on a mode of Jacobi
     // eigenvalue mu: 0 on the checkerboard, about 1 on the smooth modes the
-    // iteration is working on).
-    const bool filter = std::is_same<T, float>::value && resid;
+    // iteration is working on), in float32 at the rate of a sweep. (The same
+    // passes in FP64 on x after the update cost 3 ms per capped 4096^2 step.)
     for (;;) {
         // x_new = x + e/scale; r = b - A x_new (FP64); |r| stats
         LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
@@ -660,21 +660,6 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
                                                        s.x[1 - s.xcur], s.r, ld, w, h, s.red, s.maxabs);
         LCK(launched());
         s.xcur = 1 - s.xcur;
-        if (filter && ecur) {
-            for (int k = 0; k < PFS_START_DAMP_PASSES; ++k) {
-                k_lp_damp<<<g2(w, h), dim3(kBX, kBY), 0, st>>>(s.x[s.xcur], (const float *)s.b, s.x[1 - s.xcur], ld,
-                                                               w, h);
-                LCK(launched());
-                s.xcur = 1 - s.xcur;
-            }
-            // the residual of the filtered pressure (no correction: x is copied through)
-            LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
-            k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], (const T *)nullptr, s.escale,
-                                                           (const float *)s.b, s.x[1 - s.xcur], s.r, ld, w, h, s.red,
-                                                           s.maxabs);
-            LCK(launched());
-            s.xcur = 1 - s.xcur;
-        }
         LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
         LCK(cudaStreamSynchronize(st));
         o.checks++;
@@ -709,6 +694,12 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
                 const float *eo = nullptr;
                 const int rc = lp_correction_f32(s, p, tol_in, std::min(interval, p.max_iters - S), 0, st, n, eo, code);
                 if (rc != PFS_OK) return rc;
+                if (eo) {  // the filter: an even number of passes through the other plane ends back in eo
+                    float *ea = const_cast<float *>(eo);
+                    float *eb = (ea == (float *)s.e[0]) ? (float *)s.e[1] : (float *)s.e[0];
+                    for (int k = 0; k < PFS_START_DAMP_PASSES; ++k)
+                        LCK(launch_damp(k % 2 ? eb : ea, (const float *)s.rt, k % 2 ? ea : eb, ld, w, h, st));
+                }
                 stalled_in = code == 0 && n == interval;
                 ecur = (T *)const_cast<float *>(eo);
                 S += n;
