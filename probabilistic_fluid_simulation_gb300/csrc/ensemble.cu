@@ -85,7 +85,12 @@ struct EnsArgs {
     int stall_block;  // test hook: this block leaves at once (-1: none); see pfs_ensemble_debug_stall_block
 };
 
-constexpr int kRowsPerTask = 8;
+// Rows per task of the row phases (advection, divergence, refinement passes,
+// projection + image). Each lane walks its columns of a row one after another
+// with dependent gathers, so a task is latency-bound; one row per task spreads
+// a 2048-row member over 2,048 tasks instead of 256 (at 8 rows per task its
+// three row phases took about 2.8 ms per step, most warps idle at the barrier).
+constexpr int kRowsPerTask = 1;
 constexpr long long kBarrierSpinLimit = 1LL << 24;  // ~1-2 s with the back-off below
 
 // Grid-wide barrier with a bounded wait. Returns false (and every later call
@@ -180,6 +185,18 @@ __device__ __forceinline__ void ref_project_image_cell(const float *__restrict__
 // PFS_START_DAMP_PASSES damped passes e += (r - A e) / 8, which remove the
 // rounding noise it gathered in the modes Jacobi cannot damp (as the refined
 // session form does), then x += e, r = b - A x, and the FP64 residual decides.
+// Sum of a member's n per-task partials by one warp: lane l adds partials l,
+// l + 32, ... in order, then the shuffle tree combines the lanes (a fixed
+// order: the same sum every run); the total is on lane 0. One thread walking
+// the partials serially cost about 0.8 ms per residual check for a 2048^2
+// member (4,096 partials, one L2 round trip after another).
+__device__ __forceinline__ double sum_partials(const double *p, int n, int lane)
+{
+    double s = 0.0;
+    for (int t = lane; t < n; t += 32) s += __ldcg(p + t);
+    return warp_sum(s);
+}
+
 template <int G, int L, bool REF>
 __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
 {
@@ -213,10 +230,10 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         if (lane == 0) a.row_part[t] = s;
     }
     if (!grid_sync(a)) return;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+    for (int k = gw; k < a.nmem; k += nw) {
         const Member &m = a.mem[k];
-        double s = 0.0;
-        for (int t = 0; t < m.nrow; ++t) s += __ldcg(a.row_part + m.row_task0 + t);
+        const double s = sum_partials(a.row_part + m.row_task0, m.nrow, lane);
+        if (lane != 0) continue;
         volatile MemberState &ms = a.state[k];
         ms.bb = s;
         ms.done = 0;
@@ -250,10 +267,10 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             if (lane == 0) a.row_part[t] = acc;
         }
         if (!grid_sync(a)) return;
-        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+        for (int k = gw; k < a.nmem; k += nw) {
             const Member &m = a.mem[k];
-            double rr = 0.0;
-            for (int t = 0; t < m.nrow; ++t) rr += __ldcg(a.row_part + m.row_task0 + t);
+            const double rr = sum_partials(a.row_part + m.row_task0, m.nrow, lane);
+            if (lane != 0) continue;
             volatile MemberState &ms = a.state[k];
             const double bb = ms.bb;
             const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
@@ -304,12 +321,12 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
             if (lane == 0) a.rs_part[t] = v;
         }
         if (!grid_sync(a)) return;
-        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+        for (int k = gw; k < a.nmem; k += nw) {
             volatile MemberState &ms = a.state[k];
-            if (ms.done) continue;
+            if (__shfl_sync(0xffffffffu, ms.done, 0)) continue;  // the warp takes lane 0's reading
             const Member &m = a.mem[k];
-            double rr = 0.0;
-            for (int t = 0; t < m.rsx * m.rsy; ++t) rr += __ldcg(a.rs_part + m.rs_task0 + t);
+            const double rr = sum_partials(a.rs_part + m.rs_task0, m.rsx * m.rsy, lane);
+            if (lane != 0) continue;
             const double bb = ms.bb;
             const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
             ms.checks = ms.checks + 1;
@@ -390,12 +407,12 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
                 if (lane == 0) a.row_part[t] = acc;
             }
             if (!grid_sync(a)) return;
-            for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmem; k += gridDim.x * blockDim.x) {
+            for (int k = gw; k < a.nmem; k += nw) {
                 volatile MemberState &ms = a.state[k];
-                if (ms.done || !ms.refine) continue;
+                if (__shfl_sync(0xffffffffu, ms.done || !ms.refine, 0)) continue;  // lane 0's reading
                 const Member &m = a.mem[k];
-                double rr = 0.0;
-                for (int t = 0; t < m.nrow; ++t) rr += __ldcg(a.row_part + m.row_task0 + t);
+                const double rr = sum_partials(a.row_part + m.row_task0, m.nrow, lane);
+                if (lane != 0) continue;
                 const double bb = ms.bb;
                 const double rel = bb > 0.0 ? __dsqrt_rn(rr) / __dsqrt_rn(bb) : __dsqrt_rn(rr);
                 const bool full = s - ms.refine_start >= m.interval;
