@@ -134,28 +134,29 @@ enum { PFS_HOST = 0, PFS_DEVICE = 1 };
 /* Storage / arithmetic form of a session:
  *   PFS_PREC_F32   the reference's float32 arithmetic, bit-exact (default);
  *   PFS_PREC_BF16  velocity, image and the pressure correction stored bf16,
- *                  computed in FP32; pressure, residual and the refinement
- *                  update x += e in FP64 (iterative refinement: the same
- *                  Jacobi iteration, different rounding);
+ *                  computed in FP32; the pressure held as a pair of floats
+ *                  (about 48 significant bits), its residual and the
+ *                  refinement update x += e evaluated exactly enough in
+ *                  error-free float32 arithmetic (iterative refinement: the
+ *                  same Jacobi iteration, different rounding);
  *   PFS_PREC_F16   the same with fp16 storage (the right-hand side of each
  *                  correction solve is scaled by 1/max|r| into fp16 range);
  *   PFS_PREC_F64   every field and operation in FP64: the FP64 run of the
  *                  same method, the yardstick for the others' error;
  *   PFS_PREC_F32R  velocity, image and the pressure correction stored
  *                  float32, the correction sweeps in FP32 (the fused sweep
- *                  kernel of the F32 form), pressure and residual in FP64 by
- *                  the same refinement as BF16 / F16. Unlike F32, whose float
- *                  pressure cannot represent a solution below a relative
- *                  residual of about 4.5 * 2^-25 * rms(p) / rms(b) (about
- *                  1e-5 on a 256x256 vortex grid, more on larger ones), it
- *                  reaches any tolerance the FP64 residual resolves.
+ *                  kernel of the F32 form), the pressure pair and its
+ *                  residual by the same refinement as BF16 / F16. Unlike F32,
+ *                  whose float pressure stops falling near a relative residual
+ *                  of 1e-4 on a 256x256 vortex grid and 1e-3 at 2048x2048, it
+ *                  reaches tolerances far below 1e-5 (the pair's 48 bits).
  * The non-F32 forms run with viscosity 0 and an even diffusion count (the
  * reference's buffer roles then reduce to: pressure iteration from the
  * previous final pressure, projection with the final pressure); other
  * settings return PFS_ERR_UNSUPPORTED. check_every sets the sweeps between
  * refinements of the refined forms (0 means 32), except for F32R in residual
  * mode (tol > 0): there the correction sweeps run with the F32 form's fused
- * residual checks every check_every sweeps, and the FP64 refinement runs when
+ * residual checks every check_every sweeps, and the refinement runs when
  * the correction's residual reaches the tolerance or every 0.025 * n^2 sweeps
  * (n the larger grid side; long before the float32 correction nears its
  * rounding floor), so the refinement pass is rare and the sweeps run at the F32

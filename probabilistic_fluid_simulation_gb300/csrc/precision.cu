@@ -166,31 +166,61 @@ __global__ void __launch_bounds__(256) k_lp_divergence(const T *__restrict__ u, 
     reduce_blocks(std::is_same<C, double>::value ? accd : accf.value(), red, 1);
 }
 
+// The pressure of the refined forms (bf16, fp16, float32 storage) is an
+// unevaluated pair of floats hi + lo, about 48 significant bits, kept in the
+// 8 bytes per cell an FP64 plane takes (hi in the first half of the plane's
+// memory, lo in the second), so the refinement runs on the FP32 pipe with
+// error-free transformations instead of on GB300's FP64 pipe (which held the
+// FP64 version of this pass at 80% busy and a sixth of the HBM rate). The FP64
+// form keeps FP64 planes.
+__device__ __forceinline__ FF ff_add(FF x, float a, float a_lo)
+{
+    const FF s = two_sum(x.hi, a);
+    return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, a_lo)));
+}
+
+// r = b + xL + xR + xT + xB - 4 xc for pairs: the hi parts summed with their
+// exact rounding errors (TwoSum), the errors and lo parts summed in float.
+__device__ __forceinline__ FF ff_residual(float b, FF l, FF r, FF t, FF bo, FF c)
+{
+    FF s = two_sum(b, l.hi);
+    float e = __fadd_rn(s.lo, l.lo);
+    s = two_sum(s.hi, r.hi);
+    e = __fadd_rn(e, __fadd_rn(s.lo, r.lo));
+    s = two_sum(s.hi, t.hi);
+    e = __fadd_rn(e, __fadd_rn(s.lo, t.lo));
+    s = two_sum(s.hi, bo.hi);
+    e = __fadd_rn(e, __fadd_rn(s.lo, bo.lo));
+    s = two_sum(s.hi, __fmul_rn(-4.0f, c.hi));  // -4 hi is exact
+    e = __fadd_rn(e, __fadd_rn(s.lo, __fmul_rn(-4.0f, c.lo)));
+    return two_sum(s.hi, e);
+}
+
 // Refinement: x_out = x_in + e / scale (e may be null: no correction yet);
-// r = b - A x_out in FP64 per cell, stored as float; sum r^2 (slot 0) and
-// max |r| (as float bits, atomicMax).
-//
-// The pass is bound by GB300's FP64 pipe, not by its 26 bytes per cell, so
-// each corrected pressure is computed once: a block stages x_in + e / scale
-// for a 32 x 32 tile and its one-cell halo (periodic wrap) in shared memory,
-// then evaluates the residual from there. That is 2.3 FP64 operations per
-// cell for the correction instead of 10 when each cell recomputes its four
-// neighbours' corrected values; the results are the same bits either way.
-// Measured at 4096^2 on GB300: 372 us per pass with a bf16 correction
-// (655 us recomputing), 296 us without one (321 us).
+// r = b - A x_out per cell, stored as float; sum r^2 (slot 0) and max |r|
+// (as float bits, atomicMax). A block stages x_in + e / scale for a 32 x 32
+// tile and its one-cell halo (periodic wrap) in shared memory, so each
+// corrected pressure is formed once.
 constexpr int kRefTile = 32;
 template <typename T>
-__global__ void __launch_bounds__(256) k_lp_refine(const double *__restrict__ x_in, const T *__restrict__ e,
-                                                   const double *__restrict__ escale, const float *__restrict__ b,
-                                                   double *__restrict__ x_out, float *__restrict__ rout, int ld,
-                                                   int w, int h, Reduce red, unsigned *maxabs)
+__global__ void __launch_bounds__(256) k_lp_refine(const float *__restrict__ xh_in, const float *__restrict__ xl_in,
+                                                   const T *__restrict__ e, const double *__restrict__ escale,
+                                                   const float *__restrict__ b, float *__restrict__ xh_out,
+                                                   float *__restrict__ xl_out, float *__restrict__ rout, int ld, int w,
+                                                   int h, Reduce red, unsigned *maxabs)
 {
     constexpr int TS = kRefTile, SP = kRefTile + 2;
-    __shared__ double xs[SP][SP];
-    const double inv = e ? 1.0 / *escale : 0.0;
+    __shared__ float2 xs[SP][SP];
+    // 1 / scale as a float pair (three FP64 operations per thread)
+    float ih = 0.0f, il = 0.0f;
+    if (e) {
+        const double inv = 1.0 / *escale;
+        ih = (float)inv;
+        il = (float)(inv - (double)ih);
+    }
     const int tx = (w + TS - 1) / TS, ntiles = tx * ((h + TS - 1) / TS);
     const int lane = threadIdx.x & 31;
-    double acc = 0.0;
+    FFAcc acc;
     unsigned mx = 0u;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int i0 = (t % tx) * TS, j0 = (t / tx) * TS;
@@ -203,25 +233,28 @@ __global__ void __launch_bounds__(256) k_lp_refine(const double *__restrict__ x_
             gi = gi < 0 ? gi + w : (gi >= w ? gi - w : gi);
             gj = gj < 0 ? gj + h : (gj >= h ? gj - h : gj);
             const size_t o = (size_t)gj * ld + gi;
-            double v = x_in[o];
-            if (e) v = __fma_rn((double)Store<T>::to_f(e[o]), inv, v);
-            xs[c][a] = v;
+            FF v{xh_in[o], xl_in[o]};
+            if (e) {  // + e * (ih + il): the product and its rounding error (FMA), then added to the pair
+                const float ev = Store<T>::to_f(e[o]);
+                const float p = __fmul_rn(ev, ih);
+                v = ff_add(v, p, __fadd_rn(__fmaf_rn(ev, ih, -p), __fmul_rn(ev, il)));
+            }
+            xs[c][a] = make_float2(v.hi, v.lo);
         }
         __syncthreads();
         if (lane < iw) {
             for (int c = threadIdx.x >> 5; c < jh; c += blockDim.x >> 5) {
                 const size_t o = (size_t)(j0 + c) * ld + i0 + lane;
-                const double xc = xs[c + 1][lane + 1];
-                double q = __dadd_rn((double)b[o], xs[c + 1][lane]);
-                q = __dadd_rn(q, xs[c + 1][lane + 2]);
-                q = __dadd_rn(q, xs[c][lane + 1]);
-                q = __dadd_rn(q, xs[c + 2][lane + 1]);
-                q = __fma_rn(-4.0, xc, q);  // = q - 4 xc rounded once: 4 xc is exact
-                x_out[o] = xc;
-                const float qf = (float)q;
-                rout[o] = qf;
-                mx = max(mx, __float_as_uint(fabsf(qf)));
-                acc = __fma_rn(q, q, acc);
+                const float2 xc = xs[c + 1][lane + 1], xl = xs[c + 1][lane], xr = xs[c + 1][lane + 2];
+                const float2 xt = xs[c][lane + 1], xb = xs[c + 2][lane + 1];
+                const FF q = ff_residual(b[o], FF{xl.x, xl.y}, FF{xr.x, xr.y}, FF{xt.x, xt.y}, FF{xb.x, xb.y},
+                                         FF{xc.x, xc.y});
+                xh_out[o] = xc.x;
+                xl_out[o] = xc.y;
+                rout[o] = q.hi;
+                mx = max(mx, __float_as_uint(fabsf(q.hi)));
+                const float sq = __fmul_rn(q.hi, q.hi);
+                acc.add(sq, __fadd_rn(__fmaf_rn(q.hi, q.hi, -sq), __fmul_rn(__fmul_rn(2.0f, q.hi), q.lo)));
             }
         }
         __syncthreads();
@@ -229,7 +262,35 @@ __global__ void __launch_bounds__(256) k_lp_refine(const double *__restrict__ x_
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0 && mx) atomicMax(maxabs, mx);
-    reduce_blocks(acc, red, 0);
+    reduce_blocks(acc.value(), red, 0);
+}
+
+// Damped pass on a predicted start, pairs: x_out = x + (b - A x) / 8 (the
+// Jacobi update with weight 1/2; gain (1 + l) / 2 on a mode of Jacobi
+// eigenvalue l).
+__global__ void k_ff_damp(const float *__restrict__ xh, const float *__restrict__ xl, const float *__restrict__ b,
+                          float *__restrict__ xho, float *__restrict__ xlo, int ld, int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t r = (size_t)j * ld;
+    auto at = [&](size_t o) { return FF{xh[o], xl[o]}; };
+    const FF c = at(r + i);
+    const FF q = ff_residual(b[r + i], at(r + wm_(i, w)), at(r + wp_(i, w)), at((size_t)wm_(j, h) * ld + i),
+                             at((size_t)wp_(j, h) * ld + i), c);
+    const FF x = ff_add(c, __fmul_rn(q.hi, 0.125f), __fmul_rn(q.lo, 0.125f));
+    xho[r + i] = x.hi;
+    xlo[r + i] = x.lo;
+}
+
+// x += d (a predicted correction), pairs.
+__global__ void k_ff_add(float *__restrict__ xh, float *__restrict__ xl, const float *__restrict__ d, size_t n)
+{
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        const FF x = ff_add(FF{xh[k], xl[k]}, d[k], 0.0f);
+        xh[k] = x.hi;
+        xl[k] = x.lo;
+    }
 }
 
 // r (float) -> 16-bit right-hand side scaled by 1 / max|r|; records the scale.
@@ -280,30 +341,6 @@ __global__ void k_f64_sweep(const double *__restrict__ pin, const double *__rest
     pout[r + i] = __dmul_rn(__dadd_rn(s, b[r + i]), 0.25);
 }
 
-// Damped Jacobi pass on a predicted start, in FP64: x_out = x + (b - A x) / 8,
-// i.e. the Jacobi update with weight 1/2. Its gain on an error mode of
-// Jacobi eigenvalue l is (1 + l) / 2: zero on the checkerboard mode (l = -1),
-// which undamped sweeps carry unchanged forever, small near it, close to 1 on
-// the smooth modes.
-__global__ void k_lp_damp(const double *__restrict__ x, const float *__restrict__ b, double *__restrict__ xo, int ld,
-                          int w, int h)
-{
-    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
-    if (i >= w || j >= h) return;
-    const size_t r = (size_t)j * ld;
-    const double s = __dadd_rn(__dadd_rn(__dadd_rn(x[r + wm_(i, w)], x[r + wp_(i, w)]), x[(size_t)wm_(j, h) * ld + i]),
-                               x[(size_t)wp_(j, h) * ld + i]);
-    const double q = __dsub_rn(__dadd_rn((double)b[r + i], s), __dmul_rn(4.0, x[r + i]));
-    xo[r + i] = __fma_rn(q, 0.125, x[r + i]);
-}
-
-// x += d (a predicted correction), FP64 accumulation.
-__global__ void k_lp_add(double *__restrict__ x, const float *__restrict__ d, size_t n)
-{
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-        x[k] += (double)d[k];
-}
-
 // FP64 form: residual exactly as the oracle evaluates it, sum r^2 (slot 0).
 __global__ void __launch_bounds__(256) k_f64_residual(const double *__restrict__ p, const double *__restrict__ b,
                                                       int ld, int w, int h, Reduce red)
@@ -323,22 +360,37 @@ __global__ void __launch_bounds__(256) k_f64_residual(const double *__restrict__
     reduce_blocks(acc, red, 0);
 }
 
-// Projection (src/fluid.cpp:269-296) with the FP64 pressure: the gradient is
-// formed in C from the pressure values, ((pR - pL) * dt) / 2.
+// The pressure as the projection reads it: an FP64 plane (the FP64 form) or
+// the refined forms' float pair (hi, lo), 8 bytes per cell either way.
+struct XPlane {
+    const double *d;   // FP64 plane, or null
+    const float *hi;   // pair planes when d is null
+    const float *lo;
+    // x_a - x_b, rounded once to C
+    template <typename C>
+    __device__ __forceinline__ C diff(size_t a, size_t b) const
+    {
+        if (d) return (C)(d[a] - d[b]);
+        const FF s = two_sum(hi[a], -hi[b]);  // exact difference of the hi parts
+        return (C)__fadd_rn(s.hi, __fadd_rn(s.lo, __fsub_rn(lo[a], lo[b])));
+    }
+};
+
+// Projection (src/fluid.cpp:269-296) with the refined pressure: the gradient
+// is formed in C from the pressure values, ((pR - pL) * dt) / 2.
 template <typename C>
-__device__ __forceinline__ void lp_grad(const double *__restrict__ x, int ld, int w, int h, C dt, int i, int j, C &gx,
-                                        C &gy)
+__device__ __forceinline__ void lp_grad(const XPlane &x, int ld, int w, int h, C dt, int i, int j, C &gx, C &gy)
 {
     const size_t r = (size_t)j * ld;
-    const C dx = (C)(x[r + wp_(i, w)] - x[r + wm_(i, w)]);
-    const C dy = (C)(x[(size_t)wp_(j, h) * ld + i] - x[(size_t)wm_(j, h) * ld + i]);
+    const C dx = x.diff<C>(r + wp_(i, w), r + wm_(i, w));
+    const C dy = x.diff<C>((size_t)wp_(j, h) * ld + i, (size_t)wm_(j, h) * ld + i);
     gx = Ar<C>::div(Ar<C>::mul(dx, dt), (C)2);
     gy = Ar<C>::div(Ar<C>::mul(dy, dt), (C)2);
 }
 
 template <typename T, typename C>
-__global__ void k_lp_project(const T *__restrict__ ua, const T *__restrict__ va, const double *__restrict__ x,
-                             T *__restrict__ u, T *__restrict__ v, int ld, int w, int h, C dt)
+__global__ void k_lp_project(const T *__restrict__ ua, const T *__restrict__ va, XPlane x, T *__restrict__ u,
+                             T *__restrict__ v, int ld, int w, int h, C dt)
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
@@ -393,6 +445,17 @@ __global__ void k_lp_merge(O *__restrict__ buf, int k, int nch, const T *__restr
     buf[((size_t)j * w + i) * nch + k] = (O)x;
 }
 
+// pair planes -> interleaved O (float or double) channel k: the pair's value rounded once
+template <typename O>
+__global__ void k_ff_merge(O *__restrict__ buf, int k, int nch, const float *__restrict__ xh, const float *__restrict__ xl,
+                           int ld, int w, int h)
+{
+    const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
+    if (i >= w || j >= h) return;
+    const size_t o = (size_t)j * ld + i;
+    buf[((size_t)j * w + i) * nch + k] = (O)((double)xh[o] + (double)xl[o]);
+}
+
 inline int rup(int x, int m) { return (x + m - 1) / m * m; }
 
 }  // namespace
@@ -443,12 +506,19 @@ int lp_fail(int code, const char *msg) { return record_error(code, msg); }
         if (e_ != cudaSuccess) return lp_fail(PFS_ERR_CUDA, cudaGetErrorString(e_)); \
     } while (0)
 
+// The two float planes of a refined form's pressure kept in FP64-plane memory.
+inline float *pair_hi(const LpState &s, double *x) { return reinterpret_cast<float *>(x); }
+inline float *pair_lo(const LpState &s, double *x) { return reinterpret_cast<float *>(x) + s.plane; }
+
 template <typename T, typename C>
 int lp_velocity_and_image(LpState &s, const LpParams &p, cudaStream_t st, double *xfinal)
 {
     const int w = s.w, h = s.h, ld = s.ld;
     T *u = (T *)s.u, *v = (T *)s.v, *ua = (T *)s.ua, *va = (T *)s.va;
-    k_lp_project<T, C><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(ua, va, xfinal, u, v, ld, w, h, (C)p.dt);
+    XPlane xp;
+    if constexpr (std::is_same<T, double>::value) xp = {xfinal, nullptr, nullptr};
+    else xp = {nullptr, pair_hi(s, xfinal), pair_lo(s, xfinal)};
+    k_lp_project<T, C><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(ua, va, xp, u, v, ld, w, h, (C)p.dt);
     LCK(launched());
     if (s.ic > 0) {
         const C viw = (C)w / (C)s.iw, vih = (C)h / (C)s.ih;
@@ -470,8 +540,9 @@ template <typename T>
 int lp_residual(LpState &s, const double *x, double *xo, cudaStream_t st, double &rel)
 {
     LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
-    k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(x, (const T *)nullptr, s.escale, (const float *)s.b, xo, s.r, s.ld,
-                                                   s.w, s.h, s.red, s.maxabs);
+    k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(pair_hi(s, const_cast<double *>(x)), pair_lo(s, const_cast<double *>(x)),
+                                                   (const T *)nullptr, s.escale, (const float *)s.b, pair_hi(s, xo),
+                                                   pair_lo(s, xo), s.r, s.ld, s.w, s.h, s.red, s.maxabs);
     LCK(launched());
     LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
     LCK(cudaStreamSynchronize(st));
@@ -500,14 +571,16 @@ int lp_network_start(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
         const int rc = unet::predict_coarse(p.net, rhs, s.ld, s.pred, s.ld, s.h, s.w, p.coarsen, st);
         if (rc != PFS_OK) return rc;
         if (pass == 0) {
-            LCK(launch_widen(s.pred, s.x[s.xcur], s.plane, st));
+            LCK(cudaMemcpyAsync(pair_hi(s, s.x[s.xcur]), s.pred, s.plane * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            LCK(cudaMemsetAsync(pair_lo(s, s.x[s.xcur]), 0, s.plane * sizeof(float), st));
         } else {
-            k_lp_add<<<reduce_grid(), 256, 0, st>>>(s.x[s.xcur], s.pred, s.plane);
+            k_ff_add<<<reduce_grid(), 256, 0, st>>>(pair_hi(s, s.x[s.xcur]), pair_lo(s, s.x[s.xcur]), s.pred, s.plane);
             LCK(launched());
         }
         for (int k = 0; k < PFS_START_DAMP_PASSES; ++k) {
-            k_lp_damp<<<g2(s.w, s.h), dim3(kBX, kBY), 0, st>>>(s.x[s.xcur], (const float *)s.b, s.x[1 - s.xcur],
-                                                                 s.ld, s.w, s.h);
+            k_ff_damp<<<g2(s.w, s.h), dim3(kBX, kBY), 0, st>>>(pair_hi(s, s.x[s.xcur]), pair_lo(s, s.x[s.xcur]),
+                                                                (const float *)s.b, pair_hi(s, s.x[1 - s.xcur]),
+                                                                pair_lo(s, s.x[1 - s.xcur]), s.ld, s.w, s.h);
             LCK(launched());
             s.xcur = 1 - s.xcur;
         }
@@ -656,8 +729,9 @@ int lp_step_ir(LpState &s, const LpParams &p, cudaStream_t st, LpOut &o)
     for (;;) {
         // x_new = x + e/scale; r = b - A x_new (FP64); |r| stats
         LCK(launch_zero_small(s.maxabs, sizeof(unsigned), st));
-        k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(s.x[s.xcur], ecur, s.escale, (const float *)s.b,
-                                                       s.x[1 - s.xcur], s.r, ld, w, h, s.red, s.maxabs);
+        k_lp_refine<T><<<s.red.nblocks, 256, 0, st>>>(pair_hi(s, s.x[s.xcur]), pair_lo(s, s.x[s.xcur]), ecur, s.escale,
+                                                       (const float *)s.b, pair_hi(s, s.x[1 - s.xcur]),
+                                                       pair_lo(s, s.x[1 - s.xcur]), s.r, ld, w, h, s.red, s.maxabs);
         LCK(launched());
         s.xcur = 1 - s.xcur;
         LCK(launch_copy_small(s.red.result, s.hres_d, 2 * sizeof(double), st));
@@ -784,7 +858,12 @@ int lp_upload_t(LpState &s, const float *A, const float *B, const float *I, cuda
     const int w = s.w, h = s.h, ld = s.ld;
     k_lp_split<T><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(A, 0, 4, (T *)s.u, ld, w, h);
     k_lp_split<T><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(A, 1, 4, (T *)s.v, ld, w, h);
-    k_lp_split<double><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(B, 2, 4, s.x[0], ld, w, h);
+    if constexpr (std::is_same<T, double>::value) {
+        k_lp_split<double><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(B, 2, 4, s.x[0], ld, w, h);
+    } else {  // the pair (p, 0)
+        k_lp_split<float><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(B, 2, 4, pair_hi(s, s.x[0]), ld, w, h);
+        LCK(cudaMemsetAsync(pair_lo(s, s.x[0]), 0, s.plane * sizeof(float), st));
+    }
     LCK(launched(3));
     s.xcur = 0;
     for (int k = 0; k < s.ic; ++k) {
@@ -803,7 +882,11 @@ int lp_download_t(LpState &s, O *vp, O *img, cudaStream_t st)
     if (vp) {
         k_lp_merge<T, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 0, 4, (T *)s.u, ld, w, h);
         k_lp_merge<T, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 1, 4, (T *)s.v, ld, w, h);
-        k_lp_merge<double, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 2, 4, s.x[s.xcur], ld, w, h);
+        if constexpr (std::is_same<T, double>::value)
+            k_lp_merge<double, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 2, 4, s.x[s.xcur], ld, w, h);
+        else
+            k_ff_merge<O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 2, 4, pair_hi(s, s.x[s.xcur]), pair_lo(s, s.x[s.xcur]),
+                                                               ld, w, h);
         if (s.form == PFS_PREC_F64)
             k_lp_merge<double, O><<<g2(w, h), dim3(kBX, kBY), 0, st>>>(vp, 3, 4, (double *)s.b, ld, w, h);
         else
