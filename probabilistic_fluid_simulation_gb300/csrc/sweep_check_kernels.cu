@@ -12,7 +12,7 @@ int sweep_stream_blocks(int w, int h, int chunk)
 {
     const long long nsx = (w + 128 - 2 * 8 - 1) / (128 - 2 * 8);
     const long long nwork = nsx * ((h + chunk - 1) / chunk);
-    return (int)((nwork + 3) / 4);
+    return (int)((nwork + kStreamWarps - 1) / kStreamWarps);
 }
 
 cudaError_t launch_sweep_stream_check(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,

@@ -31,14 +31,17 @@ __device__ __forceinline__ void allow_dependent_launch() { asm volatile("griddep
 // grid reduction records the check in a.state (done at or below a.tol), as
 // the residual kernels do. `done` is set before the launch starts, so either
 // every block returns at once or none does.
+// The register cap per thread is the same for any kStreamWarps: 65536 over
+// (128 * min_blocks) threads.
 template <typename T, int G, int L, bool PREV, bool RES = false>
-__global__ void __launch_bounds__(128, RES && L >= 5 ? 2 : min_blocks<L>()) k_sweep_stream(StreamArgs<T> a)
+__global__ void __launch_bounds__(32 * kStreamWarps, (RES && L >= 5 ? 2 : min_blocks<L>()) * 4 / kStreamWarps)
+    k_sweep_stream(StreamArgs<T> a)
 {
     using V = typename Store<T>::Vec;
     extern __shared__ __align__(16) unsigned char sm_raw[];
     V *sm_rings = reinterpret_cast<V *>(sm_raw);
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int wid = blockIdx.x * 4 + wib;
+    const int wid = blockIdx.x * kStreamWarps + wib;
     grid_dependency_wait();
     allow_dependent_launch();
     if constexpr (!RES) {
@@ -57,15 +60,15 @@ __global__ void __launch_bounds__(128, RES && L >= 5 ? 2 : min_blocks<L>()) k_sw
 template <typename T, int G, int L, bool PREV, bool RES = false>
 cudaError_t launch_stream_t(const StreamArgs<T> &a, cudaStream_t st)
 {
-    constexpr int smem = Ring<T, L, RES>::bytes_per_block;
+    constexpr int smem = kStreamWarps * Ring<T, L, RES>::vecs_per_warp * Store<T>::vec_bytes;
     static std::atomic<unsigned long long> attr_done{0};  // per instantiation and device
     const cudaError_t e = smem_limit_once(k_sweep_stream<T, G, L, PREV, RES>, smem, attr_done);
     if (e != cudaSuccess) return e;
-    const int blocks = (a.nwork + 3) / 4;  // 4 warps per block: the shared rings are laid out for 4
+    const int blocks = (a.nwork + kStreamWarps - 1) / kStreamWarps;
     if (RES && blocks > a.red.nblocks) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(128);
+    cfg.blockDim = dim3(32 * kStreamWarps);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];

@@ -13,14 +13,21 @@ namespace pfs {
 namespace {
 
 // Level s+1 of the lane's four cells of row r from level s: `c` is row r
-// (horizontal neighbours from lanes l-1 / l+1), `up` row r-1, `dn` row r+1.
-// Per cell this is ((((l + r) + t) + bo) + b) * 0.25 with one rounding per
-// operation, as pfs::jacobi_p. The first add pairs values from different
-// lanes and runs as four scalar adds; the remaining adds and the scale act on
-// the aligned pairs (x, y) and (z, w) with the packed f32x2 instructions of
-// sm_100+ (__fadd2_rn / __fmul2_rn round each element to nearest, like
-// __fadd_rn), which halves their issue slots.
-__device__ __forceinline__ float4 jacobi4(const float4 &c, const float4 &up, const float4 &dn, const float4 &bb)
+// (horizontal neighbours from lanes l-1 / l+1), `up` row r-1, `dn` row r+1,
+// `bq` the quarter b/4 of row r. Per cell the reference computes
+// RN(RN(s + b) / 4) with s = ((l + r) + t) + bo rounded after each add
+// (pfs::jacobi_p); this computes the sum s the same way and then
+// RN(s * 0.25 + b/4) in one fused multiply-add. Scaling by a power of two
+// commutes with rounding to nearest in the normal range, so the two agree
+// bit for bit whenever b/4 is exact and |s + b| >= 2^-124 (or s + b = 0,
+// signed zeros included), and when s + b does not overflow: they can differ
+// only for pressures within a factor 4 of float32's subnormal range. That
+// takes a dependent rounding and a packed multiply off each level. The first
+// add pairs values from different lanes and runs as four scalar adds; the
+// rest act on the aligned pairs (x, y) and (z, w) with the packed f32x2
+// instructions of sm_100+ (__fadd2_rn / __ffma2_rn round each element to
+// nearest), which halves their issue slots.
+__device__ __forceinline__ float4 jacobi4(const float4 &c, const float4 &up, const float4 &dn, const float4 &bq)
 {
     const float lft = __shfl_up_sync(0xffffffffu, c.w, 1);
     const float rgt = __shfl_down_sync(0xffffffffu, c.x, 1);
@@ -30,11 +37,18 @@ __device__ __forceinline__ float4 jacobi4(const float4 &c, const float4 &up, con
     z = __fadd2_rn(z, make_float2(up.z, up.w));
     a = __fadd2_rn(a, make_float2(dn.x, dn.y));
     z = __fadd2_rn(z, make_float2(dn.z, dn.w));
-    a = __fadd2_rn(a, make_float2(bb.x, bb.y));
-    z = __fadd2_rn(z, make_float2(bb.z, bb.w));
     const float2 q = make_float2(0.25f, 0.25f);
-    a = __fmul2_rn(a, q);
-    z = __fmul2_rn(z, q);
+    a = __ffma2_rn(a, q, make_float2(bq.x, bq.y));
+    z = __ffma2_rn(z, q, make_float2(bq.z, bq.w));
+    return make_float4(a.x, a.y, z.x, z.y);
+}
+
+// v * s for a power of two s, on the pairs (x, y) and (z, w).
+__device__ __forceinline__ float4 scale4(const float4 &v, float s)
+{
+    const float2 q = make_float2(s, s);
+    const float2 a = __fmul2_rn(make_float2(v.x, v.y), q);
+    const float2 z = __fmul2_rn(make_float2(v.z, v.w), q);
     return make_float4(a.x, a.y, z.x, z.y);
 }
 
@@ -55,23 +69,33 @@ struct StreamArgs {
     int stall_window;    // > 0: stop when the residual stops falling (SolveState)
 };
 
-// Rows in flight per warp (cp.async prefetch depth).
-constexpr int kRP = 4;  // power of two
+// Warps per block of the standalone sweep kernel. Registers bound its
+// occupancy: each of an SM's four schedulers holds 16384 registers, so at
+// the 8-level kernel's 176 registers per thread a scheduler takes two warps
+// whatever the block size (blocks of two warps measured the same as four).
+constexpr int kStreamWarps = 4;
 
 constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
+constexpr int lcm_c(int a, int b) { return a / gcd_c(a, b) * b; }
+// The smallest divisor of u that is at least 4, else the smallest multiple of u that is.
+constexpr int ring_depth(int u, int d = 4) { return d > u ? (4 + u - 1) / u * u : (u % d == 0 ? d : ring_depth(u, d + 1)); }
 
 // Register rings of the pipeline. Level s (0..L-1) keeps rows y-s-2, y-s-1,
 // y-s in three register sets whose roles rotate with period 3; the divergence
-// rows y-1 .. y-L plus the row being loaded live in a ring of L+1 registers
-// (L+2 when the launch also evaluates the residual of level L, which needs b
-// one row further back). Unrolling the row loop by U = lcm(3, NB) makes every
-// ring index a compile-time register name: no register moves, one
-// shared-memory read of b per row instead of one per level.
+// rows y-1 .. y-L (as b/4) plus the row being loaded live in a ring of NB = L+1
+// registers (L+2 when the launch also evaluates the residual of level L,
+// which needs b one row further back). The rows copied from global memory
+// land in a shared-memory ring of D rows per plane (D-1 rows in flight).
+// Unrolling the row loop by U = lcm(3, NB, D) makes every ring index a
+// compile-time name: register rings without moves, shared-memory slots at
+// fixed offsets, one shared-memory read of b per row instead of one per level.
 template <typename T, int L, bool RES = false>
 struct Ring {
     static constexpr int NB = L + 1 + (RES ? 1 : 0);
-    static constexpr int U = 3 * NB / gcd_c(3, NB);
-    static constexpr int vecs_per_warp = 2 * kRP * 32;  // p and b prefetch rings, one vector per lane and row
+    static constexpr int UR = lcm_c(3, NB);
+    static constexpr int D = ring_depth(UR);
+    static constexpr int U = lcm_c(UR, D);
+    static constexpr int vecs_per_warp = 2 * D * 32;  // p and b rings, one vector per lane and row
     static constexpr int bytes_per_block = 4 * vecs_per_warp * Store<T>::vec_bytes;
 };
 
@@ -97,7 +121,7 @@ template <typename T>
 struct Cursor {
     const T *gp, *gb;      // next row to prefetch (p and b planes, lane column)
     int ld_row;            // its row index (wrapped)
-    long long st_off;      // offset of the level-L row of this step, in floats from the lane column
+    long long st_off;      // offset of the level-L row of this step, in elements from the lane column
     int st_rel;            // that row minus y0 (stored when 0 <= st_rel < rows)
 };
 
@@ -120,12 +144,22 @@ __device__ __forceinline__ void prefetch_row(Cursor<T> &cu, typename Store<T>::V
 }
 
 // One row step t of the pipeline (load row y = ybeg + t); K = t mod U is a
-// compile-time constant, so R[K % 3]... and bq[...] name fixed registers.
+// compile-time constant, so R[K % 3]..., bq[...] and the shared-memory slots
+// (row t in slot K % D) are fixed names. (Deriving the stored row from t
+// instead of the running st_off / st_rel measured 4% slower.)
+// T0 >= 0: t = T0 + K is known at compile time (the ramp at the start of a
+// task), and the levels whose row at this step lies outside the trapezoid the
+// stored rows need are not computed. Level s at step t produces level s+1 at
+// row ybeg + t - s - 1, and the stored rows need level s+1 from row
+// ybeg + s + 1 on (from y0 - (E - s - 1)), so it is useful from t = 2s + 2 on.
+// At 8 levels and 32-row chunks that is 72 of the 384 level rows of a task.
+// A skipped level leaves its ring slot holding an older row, which feeds only
+// rows outside the trapezoid in turn.
 // With RES, TR keeps the last three level-L rows (period 3) and the step adds
 // the exact squared residual of level L at row y-L-1 (the row stored at the
 // previous step) into acc, with the per-cell arithmetic of the residual
 // kernels (residual_sq), for the stored lanes only.
-template <typename T, int L, bool PREV, bool RES, int K>
+template <typename T, int L, bool PREV, bool RES, int K, int T0>
 __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB],
                                             float4 (&TR)[3], FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
                                             typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
@@ -133,18 +167,20 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
 {
     using V = typename Store<T>::Vec;
     constexpr int NB = Ring<T, L, RES>::NB;
+    constexpr int D = Ring<T, L, RES>::D;
     float4(&P)[L] = R[K % 3];
     float4(&Cur)[L] = R[(K + 1) % 3];
     float4(&N)[L] = R[(K + 2) % 3];
-    if (t + kRP - 1 < nsteps) prefetch_row(cu, pr, br, (t + kRP - 1) & (kRP - 1), a);
+    if (t + D - 1 < nsteps) prefetch_row(cu, pr, br, (K + D - 1) % D, a);
     cp_async_commit();
-    cp_async_wait<kRP - 1>();  // row t has landed
-    N[0] = a.pin ? Store<T>::to_f4(pr[(t & (kRP - 1)) * 32]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    bq[K % NB] = Store<T>::to_f4(br[(t & (kRP - 1)) * 32]);  // b of row y, first used at the next step
-    float4 top;
+    cp_async_wait<D - 1>();  // row t has landed
+    N[0] = Store<T>::to_f4(pr[(K % D) * 32]);  // zeros when a.pin is null (ring zero-filled)
+    bq[K % NB] = scale4(Store<T>::to_f4(br[(K % D) * 32]), 0.25f);  // b/4 of row y, used from the next step
+    float4 top = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int s = 0; s < L; ++s) {
-        const float4 &bb = bq[(K + NB * L - s - 1) % NB];  // b of row y-s-1
+        if (T0 >= 0 && T0 + K < 2 * s + 2) continue;        // compile-time: outside the trapezoid
+        const float4 &bb = bq[(K + NB * L - s - 1) % NB];  // b/4 of row y-s-1
         const float4 o = jacobi4(Cur[s], P[s], N[s], bb);   // level s+1, row y-s-1
         if (s + 1 < L) N[s + 1] = o;
         else top = o;
@@ -156,7 +192,7 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
         TR[K % 3] = top;                                  // level L, row y-L
         const float4 &c = TR[(K + 2) % 3];                // row y-L-1
         const float4 &up = TR[(K + 1) % 3];               // row y-L-2
-        const float4 &bb = bq[(K + NB * (L + 1) - L - 1) % NB];  // b of row y-L-1
+        const float4 bb = scale4(bq[(K + NB * (L + 1) - L - 1) % NB], 4.0f);  // b of row y-L-1
         const float lft = __shfl_up_sync(0xffffffffu, c.w, 1);
         const float rgt = __shfl_down_sync(0xffffffffu, c.x, 1);
         if (out && (unsigned)(cu.st_rel - 1) < (unsigned)rows) {
@@ -167,7 +203,7 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
     cu.st_rel += 1;
 }
 
-template <typename T, int L, bool PREV, bool RES, int K>
+template <typename T, int L, bool PREV, bool RES, int K, int T0>
 __device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB],
                                              float4 (&TR)[3], FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
                                              typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
@@ -175,14 +211,32 @@ __device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&
 {
     if constexpr (K < Ring<T, L, RES>::U) {
         if (t + K < nsteps) {
-            stream_step<T, L, PREV, RES, K>(t + K, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
-            stream_steps<T, L, PREV, RES, K + 1>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_step<T, L, PREV, RES, K, T0>(t + K, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+            stream_steps<T, L, PREV, RES, K + 1, T0>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
         }
     }
 }
 
-// Blocks per SM the register budget aims for: the deepest pipelines need
-// more than 65536 / (3 * 128) registers per thread without spilling.
+// The ramp: the unrolled iterations I = 0, 1, ... whose first step I * U is
+// below 2L, with their step numbers known at compile time.
+template <typename T, int L, bool PREV, bool RES, int I>
+__device__ __forceinline__ void stream_ramp(float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB], float4 (&TR)[3],
+                                            FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
+                                            typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
+                                            int nsteps, int rows, T *out, T *outp)
+{
+    constexpr int U = Ring<T, L, RES>::U;
+    if constexpr (I * U < 2 * L) {
+        stream_steps<T, L, PREV, RES, 0, I * U>(I * U, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+        stream_ramp<T, L, PREV, RES, I + 1>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    }
+}
+template <int L, int U>
+constexpr int ramp_steps() { return (2 * L + U - 1) / U * U; }
+
+// Blocks of 128 threads per SM the register budget aims for: the deepest
+// pipelines need more than 65536 / (3 * 128) registers per thread without
+// spilling.
 template <int L>
 constexpr int min_blocks() { return L >= 7 ? 2 : 3; }
 
@@ -211,8 +265,13 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     const int ybeg = y0 - E;
     const int nsteps = rows + 2 * E;
 
+    constexpr int D = Ring<T, L, RES>::D;
     V *pr = ring + lane;
-    V *br = pr + kRP * 32;
+    V *br = pr + D * 32;
+    if (!a.pin) {  // zero input iterate: no p rows are copied, the ring stays zero
+#pragma unroll
+        for (int k = 0; k < D; ++k) pr[k * 32] = V{};
+    }
 
     Cursor<T> cu;
     cu.ld_row = ybeg % a.h;
@@ -224,7 +283,7 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     T *out = st_lane ? a.pout + cx : nullptr;
     T *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
 #pragma unroll
-    for (int k = 0; k < kRP - 1; ++k) {
+    for (int k = 0; k < D - 1; ++k) {
         if (k < nsteps) prefetch_row(cu, pr, br, k, a);
         cp_async_commit();
     }
@@ -238,8 +297,10 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     for (int s = 0; s < NB; ++s) bq[s] = z;
     TR[0] = TR[1] = TR[2] = z;
 
-    for (int t = 0; t < nsteps; t += Ring<T, L, RES>::U)
-        stream_steps<T, L, PREV, RES, 0>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    constexpr int U = Ring<T, L, RES>::U;
+    stream_ramp<T, L, PREV, RES, 0>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    for (int t = ramp_steps<L, U>(); t < nsteps; t += U)
+        stream_steps<T, L, PREV, RES, 0, -1>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
     cp_async_wait<0>();
 }
 
