@@ -408,9 +408,9 @@ int pfs_residual_norms(const float *p, const float *b, int vx, int vy, int ld, d
  *
  * Same kernel and same results as pfs_residual_norms. Its cross-block scratch
  * is a fixed 10 KiB array inside the library, present on every device that
- * loads the library until the process exits. The first call on a device looks
- * up that array's device address (once per device, with the device current):
- * make that first call before any stream capture. Every call shares the array
+ * loads the library until the process exits; each call looks up its address
+ * in the current context. Not capturable in a CUDA graph: the call waits for
+ * its results (cudaStreamSynchronize). Every call shares the array
  * and clears the part that must start at zero itself; calls that overlap on
  * the GPU (different streams running at the same time) race on it, so issue
  * them one after another. Grids above 2^30 cells are rejected with

@@ -18,7 +18,6 @@
 // that overlap on the GPU (issued on different streams and running at the
 // same time) race on this array; issue them one after another.
 #include <cstdio>
-#include <mutex>
 
 #include "kernels.h"
 #include "pfs.h"
@@ -39,35 +38,21 @@ constexpr long long kNormsStaticMaxCells = 1LL << 30;
 
 static __device__ __align__(256) unsigned char g_norms_scratch[kNormsStaticBytes];
 
-// Device address of g_norms_scratch per device, looked up once per device
-// with that device current. In host code the symbol itself is only a
-// host-side stand-in, not a device address.
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void *g_scratch_addr[kMaxDevices] = {};
-
+// Device address of g_norms_scratch in the current context. In host code the
+// symbol itself is only a host-side stand-in, not a device address. It is
+// looked up on every call (cudaGetSymbolAddress allocates nothing): a cached
+// address would outlive a cudaDeviceReset, which reloads the module, and
+// would belong to another context when a second driver context is current on
+// the same device.
 int scratch_for_current_device(void **out, const char **why)
 {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) {
-        *why = "cudaGetDevice failed";
-        return PFS_ERR_NO_DEVICE;
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_norms_scratch);
+    if (e != cudaSuccess || !ptr) {
+        *why = cudaGetErrorString(e);
+        return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? PFS_ERR_NO_DEVICE : PFS_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        *why = "device ordinal out of range";
-        return PFS_ERR_UNSUPPORTED;
-    }
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void *ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_norms_scratch);
-        if (e != cudaSuccess || !ptr) {
-            *why = cudaGetErrorString(e);
-            return PFS_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = ptr;
-    }
-    *out = g_scratch_addr[dev];
+    *out = ptr;
     return PFS_OK;
 }
 
