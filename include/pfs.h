@@ -57,6 +57,19 @@ const char *pfs_last_error(void);
 int pfs_version(void);
 /* Number of CUDA kernels this library has launched since it was loaded. */
 long long pfs_kernel_launches(void);
+/* Bounds-checking build (libpfs_gb300_bounds.so) only: the timestep's kernels
+ * (fused and single sweeps, advection, diffusion, divergence, projection, image
+ * advection, residuals, layout conversion) test each global access against the
+ * extent of its buffer, skip one that falls outside (a load yields zero) and
+ * record it. This call waits for the device, then reads and clears that record
+ * over every kernel run since the previous call: out[0] the number of accesses
+ * found outside, and for the first of them out[1] its site (1 fused-sweep p
+ * row, 2 fused-sweep b row, 3 fused-sweep store, 4 fused-sweep level L-1
+ * store, 5 single sweep, 6 advection, 7 diffusion, 8 divergence, 9 residual,
+ * 10 projection, 11 image advection, 12 layout conversion, 13 auxiliary
+ * passes), out[2] its source line, out[3] its element index and out[4] the
+ * buffer's extent in elements. The normal build returns PFS_ERR_UNSUPPORTED. */
+int pfs_bounds_status(long long out[5]);
 
 /* ---- global settings --------------------------------------------------------- */
 /* Sweep count of both diffusion and pressure per step; replaces

@@ -20,6 +20,9 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpfs_gb300.so")
+# the bounds-checking build (device-side bounds checks reported by pfs_bounds_status)
+OBJDIR_BOUNDS = os.path.join(PKG, "_build_bounds")
+LIB_BOUNDS = os.path.join(PKG, "libpfs_gb300_bounds.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE, "-I", CSRC,
@@ -43,12 +46,13 @@ def headers():
     return hs
 
 
-def _compile(src: str, force: bool, verbose: bool) -> str:
-    obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+def _compile(src: str, force: bool, verbose: bool, bounds: bool = False) -> str:
+    obj = os.path.join(OBJDIR_BOUNDS if bounds else OBJDIR, os.path.basename(src) + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers()])
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-DPFS_BOUNDS_CHECK"] if bounds else []) + \
+        (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -87,23 +91,28 @@ def build_cli(force: bool = False) -> str:
     return CLI_BIN
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(OBJDIR, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, bounds: bool = False) -> str:
+    """Build libpfs_gb300.so (and the CLI), or with bounds=True the
+    bounds-checking libpfs_gb300_bounds.so (same sources, PFS_BOUNDS_CHECK)."""
+    objdir, lib = (OBJDIR_BOUNDS, LIB_BOUNDS) if bounds else (OBJDIR, LIB)
+    os.makedirs(objdir, exist_ok=True)
     srcs = sources()
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, force, verbose), srcs))
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        objs = list(ex.map(lambda s: _compile(s, force, verbose, bounds), srcs))
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    build_cli(force)
-    return LIB
+    if not bounds:
+        build_cli(force)
+    return lib
 
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--bounds", action="store_true", help="the bounds-checking library")
     a = ap.parse_args()
-    print(build(force=a.force, verbose=a.verbose))
+    print(build(force=a.force, verbose=a.verbose, bounds=a.bounds))

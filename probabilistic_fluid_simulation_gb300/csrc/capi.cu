@@ -20,7 +20,9 @@
 #include <new>
 #include <string>
 #include <utility>
+#include <vector>
 
+#include "bounds.cuh"
 #include "kernels.h"
 #include "nvtx.h"
 #include "pfs.h"
@@ -673,6 +675,61 @@ const char *pfs_last_error(void) { return g_err.c_str(); }
 int pfs_version(void) { return 200; }
 
 long long pfs_kernel_launches(void) { return pfs::g_launches.load(std::memory_order_relaxed); }
+
+#ifdef PFS_BOUNDS_CHECK
+extern "C++" {
+namespace pfs {
+namespace {
+struct BoundsUnit {
+    int (*read)(BoundsRecord *, bool);
+    const char *unit;
+};
+std::mutex &bounds_mu()
+{
+    static std::mutex m;
+    return m;
+}
+std::vector<BoundsUnit> &bounds_units()
+{
+    static std::vector<BoundsUnit> v;
+    return v;
+}
+}  // namespace
+void bounds_register(int (*read)(BoundsRecord *, bool), const char *unit)
+{
+    std::lock_guard<std::mutex> lk(bounds_mu());
+    bounds_units().push_back({read, unit});
+}
+}  // namespace pfs
+}  // extern "C++"
+#endif
+
+int pfs_bounds_status(long long out[5])
+{
+#ifndef PFS_BOUNDS_CHECK
+    (void)out;
+    return fail(PFS_ERR_UNSUPPORTED, "this build has no bounds checks (libpfs_gb300_bounds.so has them)");
+#else
+    if (!out) return fail(PFS_ERR_INVALID_ARGUMENT, "null output");
+    for (int k = 0; k < 5; ++k) out[k] = 0;
+    const cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(PFS_ERR_CUDA, "cudaDeviceSynchronize: %s", cudaGetErrorString(e));
+    std::lock_guard<std::mutex> lk(pfs::bounds_mu());
+    for (const pfs::BoundsUnit &u : pfs::bounds_units()) {
+        pfs::BoundsRecord r{};
+        if (u.read(&r, true) != 0) return fail(PFS_ERR_CUDA, "reading the bounds record of %s failed", u.unit);
+        if (r.count == 0) continue;
+        if (out[0] == 0) {
+            out[1] = r.site;
+            out[2] = r.line;
+            out[3] = r.index;
+            out[4] = r.extent;
+        }
+        out[0] += (long long)r.count;
+    }
+    return PFS_OK;
+#endif
+}
 
 int pfs_set_jacobi_iters(int n)
 {

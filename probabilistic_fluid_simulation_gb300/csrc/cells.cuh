@@ -4,6 +4,7 @@
 // reference's operation order (src/fluid.cpp, cited per function).
 #pragma once
 
+#include "bounds.cuh"
 #include "common.cuh"
 #include "reduce.cuh"
 
@@ -67,15 +68,24 @@ __device__ __forceinline__ void advect_cell(const float *__restrict__ u, const f
                                             float dt, int i, int j)
 {
     const size_t o = (size_t)j * ld + i;
+    const long long n = (long long)ld * h;  // plane extent (checked build)
+    (void)n;
     if (BC == 2 && on_edge(i, j, w, h)) {
-        uo[o] = 0.0f;
-        vo[o] = 0.0f;
+        PFS_ST(uo, o, n, 0.0f, kBsAdvect);
+        PFS_ST(vo, o, n, 0.0f, kBsAdvect);
         return;
     }
-    const Corners c = backtrace<BC>(i, j, dt, dt, u[o], v[o], (float)w, (float)h, w, h);
+    const Corners c = backtrace<BC>(i, j, dt, dt, PFS_LD(u, o, n, kBsAdvect), PFS_LD(v, o, n, kBsAdvect), (float)w,
+                                    (float)h, w, h);
     const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
-    uo[o] = bilerp(c.sx, c.sy, u[r0 + c.i0], u[r0 + c.i1], u[r1 + c.i0], u[r1 + c.i1]);
-    vo[o] = bilerp(c.sx, c.sy, v[r0 + c.i0], v[r0 + c.i1], v[r1 + c.i0], v[r1 + c.i1]);
+    PFS_ST(uo, o, n,
+           bilerp(c.sx, c.sy, PFS_LD(u, r0 + c.i0, n, kBsAdvect), PFS_LD(u, r0 + c.i1, n, kBsAdvect),
+                  PFS_LD(u, r1 + c.i0, n, kBsAdvect), PFS_LD(u, r1 + c.i1, n, kBsAdvect)),
+           kBsAdvect);
+    PFS_ST(vo, o, n,
+           bilerp(c.sx, c.sy, PFS_LD(v, r0 + c.i0, n, kBsAdvect), PFS_LD(v, r0 + c.i1, n, kBsAdvect),
+                  PFS_LD(v, r1 + c.i0, n, kBsAdvect), PFS_LD(v, r1 + c.i1, n, kBsAdvect)),
+           kBsAdvect);
 }
 
 // Divergence of cell (i, j) into b, src/fluid.cpp:218-237; returns it.
@@ -84,10 +94,13 @@ __device__ __forceinline__ float divergence_cell(const float *__restrict__ u, co
                                                  int j)
 {
     const size_t r = (size_t)j * ld;
-    const float du = fsub(u[r + wp(i, w)], u[r + wm(i, w)]);
-    const float dv = fsub(v[(size_t)wp(j, h) * ld + i], v[(size_t)wm(j, h) * ld + i]);
+    const long long n = (long long)ld * h;
+    (void)n;
+    const float du = fsub(PFS_LD(u, r + wp(i, w), n, kBsDivergence), PFS_LD(u, r + wm(i, w), n, kBsDivergence));
+    const float dv = fsub(PFS_LD(v, (size_t)wp(j, h) * ld + i, n, kBsDivergence),
+                          PFS_LD(v, (size_t)wm(j, h) * ld + i, n, kBsDivergence));
     const float bv = fmul(gamma, fadd(du, dv));
-    b[r + i] = bv;
+    PFS_ST(b, r + i, n, bv, kBsDivergence);
     return bv;
 }
 
@@ -156,10 +169,16 @@ __device__ __forceinline__ void project_cell(const float *__restrict__ u, const 
                                              int j, float &uo, float &vo)
 {
     const size_t r = (size_t)j * ld;
-    const float gx = fmul(fmul(fsub(p[r + wp(i, w)], p[r + wm(i, w)]), dt), 0.5f);
-    const float gy = fmul(fmul(fsub(p[(size_t)wp(j, h) * ld + i], p[(size_t)wm(j, h) * ld + i]), dt), 0.5f);
-    uo = fsub(u[r + i], gx);
-    vo = fsub(v[r + i], gy);
+    const long long n = (long long)ld * h;
+    (void)n;
+    const float gx =
+        fmul(fmul(fsub(PFS_LD(p, r + wp(i, w), n, kBsProject), PFS_LD(p, r + wm(i, w), n, kBsProject)), dt), 0.5f);
+    const float gy = fmul(fmul(fsub(PFS_LD(p, (size_t)wp(j, h) * ld + i, n, kBsProject),
+                                    PFS_LD(p, (size_t)wm(j, h) * ld + i, n, kBsProject)),
+                               dt),
+                          0.5f);
+    uo = fsub(PFS_LD(u, r + i, n, kBsProject), gx);
+    vo = fsub(PFS_LD(v, r + i, n, kBsProject), gy);
     if (BC == 2 && on_edge(i, j, w, h)) {
         uo = 0.0f;
         vo = 0.0f;
@@ -178,13 +197,19 @@ __device__ __forceinline__ void project_image_cell(const float *__restrict__ u, 
     float un, vn;
     project_cell<BC>(u, v, p, ld, w, h, dt, i, j, un, vn);
     const size_t o = (size_t)j * ld + i;
-    uo[o] = un;
-    vo[o] = vn;
+    const long long n = (long long)ld * h, ni = (long long)plane * c;  // velocity plane, image planes
+    (void)n;
+    (void)ni;
+    PFS_ST(uo, o, n, un, kBsProject);
+    PFS_ST(vo, o, n, vn, kBsProject);
     const Corners k = backtrace<BC>(i, j, dt, dt, un, vn, (float)w, (float)h, w, h);
     const size_t r0 = (size_t)k.j0 * ld, r1 = (size_t)k.j1 * ld;
     for (int ch = 0; ch < c; ++ch) {
-        const float *s = img + ch * plane;
-        imgo[ch * plane + o] = bilerp(k.sx, k.sy, s[r0 + k.i0], s[r0 + k.i1], s[r1 + k.i0], s[r1 + k.i1]);
+        const size_t s = ch * plane;
+        PFS_ST(imgo, s + o, ni,
+               bilerp(k.sx, k.sy, PFS_LD(img, s + r0 + k.i0, ni, kBsImage), PFS_LD(img, s + r0 + k.i1, ni, kBsImage),
+                      PFS_LD(img, s + r1 + k.i0, ni, kBsImage), PFS_LD(img, s + r1 + k.i1, ni, kBsImage)),
+               kBsImage);
     }
 }
 
@@ -203,16 +228,23 @@ __device__ __forceinline__ void residual_strip_task(const float *__restrict__ p,
     const int xr = (sx * 128 + 4 * (last_lane + 1)) % w;    // right outside neighbour
     // loads bypass L1 (ld.global.cg): inside the persistent ensemble kernel the
     // pressure planes are rewritten by other blocks between checks
-    const float *pc = p + xs;
-    float4 up = __ldcg(reinterpret_cast<const float4 *>(pc + (size_t)wm(y0, h) * ld));
-    float4 cu = __ldcg(reinterpret_cast<const float4 *>(pc + (size_t)y0 * ld));
+    const long long n = (long long)ld * h;
+    (void)n;
+    // four floats of plane q from element k (k checked against the plane in the checked build)
+    auto row4 = [&](const float *q, size_t k) {
+        return PFS_SPAN(k, 4, n, kBsResidual) ? __ldcg(reinterpret_cast<const float4 *>(q + k))
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    auto one = [&](size_t k) { return PFS_SPAN(k, 1, n, kBsResidual) ? __ldcg(p + k) : 0.0f; };
+    float4 up = row4(p, xs + (size_t)wm(y0, h) * ld);
+    float4 cu = row4(p, xs + (size_t)y0 * ld);
     for (int y = y0; y < y1; ++y) {
-        const float4 dn = __ldcg(reinterpret_cast<const float4 *>(pc + (size_t)wp(y, h) * ld));
-        const float4 bb = __ldcg(reinterpret_cast<const float4 *>(b + (size_t)y * ld + xs));
+        const float4 dn = row4(p, xs + (size_t)wp(y, h) * ld);
+        const float4 bb = row4(b, (size_t)y * ld + xs);
         float lft = __shfl_up_sync(0xffffffffu, cu.w, 1);
         float rgt = __shfl_down_sync(0xffffffffu, cu.x, 1);
-        if (lane == 0) lft = __ldcg(p + (size_t)y * ld + xl);
-        if (lane == last_lane) rgt = __ldcg(p + (size_t)y * ld + xr);
+        if (lane == 0) lft = one((size_t)y * ld + xl);
+        if (lane == last_lane) rgt = one((size_t)y * ld + xr);
         if (active) {
             residual_sq4(acc, bb, lft, cu, rgt, up, dn);
             if (accb) {

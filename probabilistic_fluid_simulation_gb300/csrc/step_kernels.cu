@@ -34,8 +34,16 @@ __global__ void k_diffuse(const float *__restrict__ u, const float *__restrict__
     if (i >= w || j >= h) return;
     const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
     const int im = wm(i, w), ip = wp(i, w);
-    uo[r + i] = jacobi_d(u[r + im], u[r + ip], u[rm + i], u[rp + i], u[r + i], alpha, beta);
-    vo[r + i] = jacobi_d(v[r + im], v[r + ip], v[rm + i], v[rp + i], v[r + i], alpha, beta);
+    const long long n = (long long)ld * h;
+    (void)n;
+    PFS_ST(uo, r + i, n,
+           jacobi_d(PFS_LD(u, r + im, n, kBsDiffuse), PFS_LD(u, r + ip, n, kBsDiffuse), PFS_LD(u, rm + i, n, kBsDiffuse),
+                    PFS_LD(u, rp + i, n, kBsDiffuse), PFS_LD(u, r + i, n, kBsDiffuse), alpha, beta),
+           kBsDiffuse);
+    PFS_ST(vo, r + i, n,
+           jacobi_d(PFS_LD(v, r + im, n, kBsDiffuse), PFS_LD(v, r + ip, n, kBsDiffuse), PFS_LD(v, rm + i, n, kBsDiffuse),
+                    PFS_LD(v, rp + i, n, kBsDiffuse), PFS_LD(v, r + i, n, kBsDiffuse), alpha, beta),
+           kBsDiffuse);
 }
 
 // Divergence, src/fluid.cpp:218-237 (gamma = (float)(-1.0/dt) from the host);
@@ -57,10 +65,14 @@ __global__ void __launch_bounds__(256) k_residual(const float *__restrict__ p, c
 {
     if (state && *(volatile int *)&state->done) return;  // same answer for every block
     FFAcc acc;
+    const long long n = (long long)ld * h;
+    (void)n;
     for (int j = blockIdx.x; j < h; j += gridDim.x) {
         const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
         for (int i = threadIdx.x; i < w; i += blockDim.x)
-            residual_sq(acc, b[r + i], p[r + wm(i, w)], p[r + wp(i, w)], p[rm + i], p[rp + i], p[r + i]);
+            residual_sq(acc, PFS_LD(b, r + i, n, kBsResidual), PFS_LD(p, r + wm(i, w), n, kBsResidual),
+                        PFS_LD(p, r + wp(i, w), n, kBsResidual), PFS_LD(p, rm + i, n, kBsResidual),
+                        PFS_LD(p, rp + i, n, kBsResidual), PFS_LD(p, r + i, n, kBsResidual));
     }
     reduce_blocks(acc.value(), red, 0, state, sweeps_here, tol, stall_window);
 }
@@ -69,11 +81,15 @@ __global__ void __launch_bounds__(256) k_norms(const float *__restrict__ p, cons
                                                int h, Reduce red)
 {
     FFAcc acc, accb;
+    const long long n = (long long)ld * h;
+    (void)n;
     for (int j = blockIdx.x; j < h; j += gridDim.x) {
         const size_t r = (size_t)j * ld, rm = (size_t)wm(j, h) * ld, rp = (size_t)wp(j, h) * ld;
         for (int i = threadIdx.x; i < w; i += blockDim.x) {
-            const float bv = b[r + i];
-            residual_sq(acc, bv, p[r + wm(i, w)], p[r + wp(i, w)], p[rm + i], p[rp + i], p[r + i]);
+            const float bv = PFS_LD(b, r + i, n, kBsResidual);
+            residual_sq(acc, bv, PFS_LD(p, r + wm(i, w), n, kBsResidual), PFS_LD(p, r + wp(i, w), n, kBsResidual),
+                        PFS_LD(p, rm + i, n, kBsResidual), PFS_LD(p, rp + i, n, kBsResidual),
+                        PFS_LD(p, r + i, n, kBsResidual));
             acc_square(accb, bv);
         }
     }
@@ -120,8 +136,8 @@ __global__ void k_project(const float *__restrict__ u, const float *__restrict__
     if (i >= w || j >= h) return;
     float a, c;
     project_cell<BC>(u, v, p, ld, w, h, dt, i, j, a, c);
-    uo[(size_t)j * ld + i] = a;
-    vo[(size_t)j * ld + i] = c;
+    PFS_ST(uo, (size_t)j * ld + i, (long long)ld * h, a, kBsProject);
+    PFS_ST(vo, (size_t)j * ld + i, (long long)ld * h, c, kBsProject);
 }
 
 // Projection, then image advection (src/fluid.cpp:72-127) of the pixel at the
@@ -151,11 +167,18 @@ __global__ void k_advect_image_planar(const float *__restrict__ img, float *__re
     const int vi = min(__float2int_rz(fmul((float)i, viw)), vw - 1);
     const int vj = min(__float2int_rz(fmul((float)j, vih)), vh - 1);
     const size_t vo = (size_t)vj * vld + vi;
-    const Corners k = backtrace<BC>(i, j, kx, ky, u[vo], v[vo], (float)iw, (float)ih, iw, ih);
+    const long long nv = (long long)vld * vh, ni = (long long)plane * c;
+    (void)nv;
+    (void)ni;
+    const Corners k = backtrace<BC>(i, j, kx, ky, PFS_LD(u, vo, nv, kBsImage), PFS_LD(v, vo, nv, kBsImage), (float)iw,
+                                    (float)ih, iw, ih);
     const size_t r0 = (size_t)k.j0 * ild, r1 = (size_t)k.j1 * ild, o = (size_t)j * ild + i;
     for (int ch = 0; ch < c; ++ch) {
-        const float *s = img + ch * plane;
-        imgo[ch * plane + o] = bilerp(k.sx, k.sy, s[r0 + k.i0], s[r0 + k.i1], s[r1 + k.i0], s[r1 + k.i1]);
+        const size_t s = ch * plane;
+        PFS_ST(imgo, s + o, ni,
+               bilerp(k.sx, k.sy, PFS_LD(img, s + r0 + k.i0, ni, kBsImage), PFS_LD(img, s + r0 + k.i1, ni, kBsImage),
+                      PFS_LD(img, s + r1 + k.i0, ni, kBsImage), PFS_LD(img, s + r1 + k.i1, ni, kBsImage)),
+               kBsImage);
     }
 }
 
@@ -168,13 +191,21 @@ __global__ void k_advect_image_interleaved(const float *__restrict__ img, float 
     if (i >= iw || j >= ih) return;
     const int vi = min(__float2int_rz(fmul((float)i, viw)), vw - 1);
     const int vj = min(__float2int_rz(fmul((float)j, vih)), vh - 1);
-    const float2 uv = *reinterpret_cast<const float2 *>(vel + ((size_t)vj * vw + vi) * 4);
+    const size_t vk = ((size_t)vj * vw + vi) * 4;
+    const long long ni = (long long)iw * ih * c;
+    (void)ni;
+    const float2 uv = PFS_SPAN(vk, 2, (long long)vw * vh * 4, kBsImage)
+                          ? *reinterpret_cast<const float2 *>(vel + vk)
+                          : make_float2(0.0f, 0.0f);
     const Corners k = backtrace(i, j, kx, ky, uv.x, uv.y, (float)iw, (float)ih, iw, ih);
     const size_t c00 = ((size_t)k.j0 * iw + k.i0) * c, c10 = ((size_t)k.j0 * iw + k.i1) * c;
     const size_t c01 = ((size_t)k.j1 * iw + k.i0) * c, c11 = ((size_t)k.j1 * iw + k.i1) * c;
     const size_t o = ((size_t)j * iw + i) * c;
     for (int ch = 0; ch < c; ++ch)
-        imgo[o + ch] = bilerp(k.sx, k.sy, img[c00 + ch], img[c10 + ch], img[c01 + ch], img[c11 + ch]);
+        PFS_ST(imgo, o + ch, ni,
+               bilerp(k.sx, k.sy, PFS_LD(img, c00 + ch, ni, kBsImage), PFS_LD(img, c10 + ch, ni, kBsImage),
+                      PFS_LD(img, c01 + ch, ni, kBsImage), PFS_LD(img, c11 + ch, ni, kBsImage)),
+               kBsImage);
 }
 
 __global__ void k_split_velocity(const float4 *__restrict__ vp, float *__restrict__ u, float *__restrict__ v, int ld,
@@ -182,9 +213,11 @@ __global__ void k_split_velocity(const float4 *__restrict__ vp, float *__restric
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    const float4 q = vp[(size_t)j * w + i];
-    u[(size_t)j * ld + i] = q.x;
-    v[(size_t)j * ld + i] = q.y;
+    const long long n = (long long)ld * h;
+    (void)n;
+    const float4 q = PFS_LD(vp, (size_t)j * w + i, (long long)w * h, kBsLayout);
+    PFS_ST(u, (size_t)j * ld + i, n, q.x, kBsLayout);
+    PFS_ST(v, (size_t)j * ld + i, n, q.y, kBsLayout);
 }
 
 __global__ void k_split_channel(const float *__restrict__ buf, int ch, int nch, float *__restrict__ plane, int ld,
@@ -192,7 +225,8 @@ __global__ void k_split_channel(const float *__restrict__ buf, int ch, int nch, 
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    plane[(size_t)j * ld + i] = buf[((size_t)j * w + i) * nch + ch];
+    PFS_ST(plane, (size_t)j * ld + i, (long long)ld * h,
+           PFS_LD(buf, ((size_t)j * w + i) * nch + ch, (long long)w * h * nch, kBsLayout), kBsLayout);
 }
 
 // One interleaved (u, v, p, b) buffer into its planes, each cell read once
@@ -203,12 +237,14 @@ __global__ void k_split_vp(const float4 *__restrict__ vp, float *__restrict__ u,
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    const float4 q = vp[(size_t)j * w + i];
+    const float4 q = PFS_LD(vp, (size_t)j * w + i, (long long)w * h, kBsLayout);
     const size_t o = (size_t)j * ld + i;
-    u[o] = q.x;
-    v[o] = q.y;
-    p[o] = q.z;
-    if (b) b[o] = q.w;
+    const long long n = (long long)ld * h;
+    (void)n;
+    PFS_ST(u, o, n, q.x, kBsLayout);
+    PFS_ST(v, o, n, q.y, kBsLayout);
+    PFS_ST(p, o, n, q.z, kBsLayout);
+    if (b) PFS_ST(b, o, n, q.w, kBsLayout);
 }
 
 __global__ void k_merge_velocity(float4 *__restrict__ out, const float *__restrict__ u, const float *__restrict__ v,
@@ -217,7 +253,12 @@ __global__ void k_merge_velocity(float4 *__restrict__ out, const float *__restri
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
     const size_t o = (size_t)j * ld + i;
-    out[(size_t)j * w + i] = make_float4(u[o], v[o], p[o], b[o]);
+    const long long n = (long long)ld * h;
+    (void)n;
+    PFS_ST(out, (size_t)j * w + i, (long long)w * h,
+           make_float4(PFS_LD(u, o, n, kBsLayout), PFS_LD(v, o, n, kBsLayout), PFS_LD(p, o, n, kBsLayout),
+                       PFS_LD(b, o, n, kBsLayout)),
+           kBsLayout);
 }
 
 __global__ void k_split_image(const float *__restrict__ img, float *__restrict__ planes, size_t plane, int ld, int w,
@@ -225,7 +266,9 @@ __global__ void k_split_image(const float *__restrict__ img, float *__restrict__
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    for (int ch = 0; ch < c; ++ch) planes[ch * plane + (size_t)j * ld + i] = img[((size_t)j * w + i) * c + ch];
+    for (int ch = 0; ch < c; ++ch)
+        PFS_ST(planes, ch * plane + (size_t)j * ld + i, (long long)plane * c,
+               PFS_LD(img, ((size_t)j * w + i) * c + ch, (long long)w * h * c, kBsLayout), kBsLayout);
 }
 
 __global__ void k_merge_image(float *__restrict__ img, const float *__restrict__ planes, size_t plane, int ld, int w,
@@ -233,7 +276,9 @@ __global__ void k_merge_image(float *__restrict__ img, const float *__restrict__
 {
     const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y;
     if (i >= w || j >= h) return;
-    for (int ch = 0; ch < c; ++ch) img[((size_t)j * w + i) * c + ch] = planes[ch * plane + (size_t)j * ld + i];
+    for (int ch = 0; ch < c; ++ch)
+        PFS_ST(img, ((size_t)j * w + i) * c + ch, (long long)w * h * c,
+               PFS_LD(planes, ch * plane + (size_t)j * ld + i, (long long)plane * c, kBsLayout), kBsLayout);
 }
 
 }  // namespace
@@ -241,7 +286,7 @@ __global__ void k_merge_image(float *__restrict__ img, const float *__restrict__
 __global__ void k_widen(const float *__restrict__ in, double *__restrict__ out, size_t n)
 {
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-        out[k] = (double)in[k];
+        PFS_ST(out, k, n, (double)PFS_LD(in, k, n, kBsAux), kBsAux);
 }
 
 cudaError_t launch_widen(const float *in, double *out, size_t n, cudaStream_t st)
@@ -262,10 +307,15 @@ __global__ void k_damp(const float *__restrict__ pin, const float *__restrict__ 
     const size_t r = (size_t)j * ld;
     const int im = i == 0 ? w - 1 : i - 1, ip = i + 1 == w ? 0 : i + 1;
     const int jm = j == 0 ? h - 1 : j - 1, jp = j + 1 == h ? 0 : j + 1;
-    const float q = fsub(fadd(fadd(fadd(fadd(b[r + i], pin[r + im]), pin[r + ip]), pin[(size_t)jm * ld + i]),
-                              pin[(size_t)jp * ld + i]),
-                         fmul(4.0f, pin[r + i]));
-    pout[r + i] = fadd(pin[r + i], fmul(q, 0.125f));
+    const long long n = (long long)ld * h;
+    (void)n;
+    const float c = PFS_LD(pin, r + i, n, kBsAux);
+    const float q = fsub(fadd(fadd(fadd(fadd(PFS_LD(b, r + i, n, kBsAux), PFS_LD(pin, r + im, n, kBsAux)),
+                                        PFS_LD(pin, r + ip, n, kBsAux)),
+                                   PFS_LD(pin, (size_t)jm * ld + i, n, kBsAux)),
+                              PFS_LD(pin, (size_t)jp * ld + i, n, kBsAux)),
+                         fmul(4.0f, c));
+    PFS_ST(pout, r + i, n, fadd(c, fmul(q, 0.125f)), kBsAux);
 }
 
 cudaError_t launch_damp(const float *pin, const float *b, float *pout, int ld, int w, int h, cudaStream_t st)
@@ -283,8 +333,15 @@ __global__ void k_residual_field(const float *__restrict__ p, const float *__res
     const size_t o = (size_t)j * ld;
     const int im = i == 0 ? w - 1 : i - 1, ip = i + 1 == w ? 0 : i + 1;
     const int jm = j == 0 ? h - 1 : j - 1, jp = j + 1 == h ? 0 : j + 1;
-    r[o + i] = fsub(fadd(fadd(fadd(fadd(b[o + i], p[o + im]), p[o + ip]), p[(size_t)jm * ld + i]), p[(size_t)jp * ld + i]),
-                    fmul(4.0f, p[o + i]));
+    const long long n = (long long)ld * h;
+    (void)n;
+    PFS_ST(r, o + i, n,
+           fsub(fadd(fadd(fadd(fadd(PFS_LD(b, o + i, n, kBsAux), PFS_LD(p, o + im, n, kBsAux)),
+                               PFS_LD(p, o + ip, n, kBsAux)),
+                          PFS_LD(p, (size_t)jm * ld + i, n, kBsAux)),
+                     PFS_LD(p, (size_t)jp * ld + i, n, kBsAux)),
+                fmul(4.0f, PFS_LD(p, o + i, n, kBsAux))),
+           kBsAux);
 }
 
 cudaError_t launch_residual_field(const float *p, const float *b, float *r, int ld, int w, int h, cudaStream_t st)
@@ -296,7 +353,7 @@ cudaError_t launch_residual_field(const float *p, const float *b, float *r, int 
 __global__ void k_add(float *__restrict__ p, const float *__restrict__ d, size_t n)
 {
     for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-        p[k] = fadd(p[k], d[k]);
+        PFS_ST(p, k, n, fadd(PFS_LD(p, k, n, kBsAux), PFS_LD(d, k, n, kBsAux)), kBsAux);
 }
 
 cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
@@ -310,7 +367,7 @@ cudaError_t launch_add(float *p, const float *d, size_t n, cudaStream_t st)
 // (a stream or event synchronisation).
 __global__ void k_small_words(const unsigned *__restrict__ src, unsigned *__restrict__ dst, int words)
 {
-    for (int k = threadIdx.x; k < words; k += 32) dst[k] = src ? src[k] : 0u;
+    for (int k = threadIdx.x; k < words; k += 32) PFS_ST(dst, k, words, src ? PFS_LD(src, k, words, kBsAux) : 0u, kBsAux);
 }
 
 cudaError_t launch_copy_small(const void *src, void *dst, size_t bytes, cudaStream_t st)

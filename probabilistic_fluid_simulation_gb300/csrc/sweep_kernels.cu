@@ -14,8 +14,10 @@
 //                   other. Global traffic per launch: read p and b once, write
 //                   p once (plus the second-to-last level when asked).
 //
-// Arithmetic per cell is pfs::jacobi_p, bit-identical to the reference, and a
-// Jacobi sweep is order-independent, so any fusion depth gives the same bits.
+// Arithmetic per cell is pfs::jacobi_p, bit-identical to the reference (the
+// fused kernel's final multiply-add on b/4 equals it throughout float32's
+// normal range, see jacobi4), and a Jacobi sweep is order-independent, so any
+// fusion depth gives the same bits.
 #include "common.cuh"
 #include "kernels.h"
 #include "storage.cuh"
@@ -33,8 +35,13 @@ __global__ void k_sweep_single(const float *__restrict__ pin, const float *__res
     const int im = (i == 0) ? w - 1 : i - 1, ip = (i + 1 == w) ? 0 : i + 1;
     const int jm = (j == 0) ? h - 1 : j - 1, jp = (j + 1 == h) ? 0 : j + 1;
     const size_t row = (size_t)j * ld;
-    pout[row + i] = jacobi_p(pin[row + im], pin[row + ip], pin[(size_t)jm * ld + i], pin[(size_t)jp * ld + i],
-                             b[row + i]);
+    const long long n = (long long)ld * h;
+    (void)n;
+    PFS_ST(pout, row + i, n,
+           jacobi_p(PFS_LD(pin, row + im, n, kBsSweepSingle), PFS_LD(pin, row + ip, n, kBsSweepSingle),
+                    PFS_LD(pin, (size_t)jm * ld + i, n, kBsSweepSingle),
+                    PFS_LD(pin, (size_t)jp * ld + i, n, kBsSweepSingle), PFS_LD(b, row + i, n, kBsSweepSingle)),
+           kBsSweepSingle);
 }
 
 int stream_strip_width(int halo) { return 128 - 2 * halo; }

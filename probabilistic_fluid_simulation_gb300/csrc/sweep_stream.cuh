@@ -3,6 +3,7 @@
 // (ensemble.cu). See sweep_kernels.cu for the design.
 #pragma once
 
+#include "bounds.cuh"
 #include "cells.cuh"
 #include "common.cuh"
 #include "kernels.h"
@@ -131,8 +132,10 @@ __device__ __forceinline__ void prefetch_row(Cursor<T> &cu, typename Store<T>::V
                                              int slot, const StreamArgs<T> &a)
 {
     constexpr int VB = Store<T>::vec_bytes;
-    if (a.pin) cp_async<VB>(pr + slot * 32, cu.gp);
-    cp_async<VB>(br + slot * 32, cu.gb);
+    const long long n = (long long)a.ld * a.h;  // plane extent (checked build)
+    (void)n;
+    if (a.pin && PFS_SPAN(cu.gp - a.pin, 4, n, kBsSweepLoadP)) cp_async<VB>(pr + slot * 32, cu.gp);
+    if (PFS_SPAN(cu.gb - a.b, 4, n, kBsSweepLoadB)) cp_async<VB>(br + slot * 32, cu.gb);
     if (++cu.ld_row == a.h) {
         cu.ld_row = 0;
         cu.gp -= (size_t)(a.h - 1) * a.ld;
@@ -185,8 +188,11 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
         if (s + 1 < L) N[s + 1] = o;
         else top = o;
     }
-    if (out && (unsigned)cu.st_rel < (unsigned)rows) *reinterpret_cast<V *>(out + cu.st_off) = Store<T>::from_f4(top);
-    if (PREV && outp && (unsigned)(cu.st_rel + 1) < (unsigned)rows)
+    if (out && (unsigned)cu.st_rel < (unsigned)rows &&
+        PFS_SPAN(out + cu.st_off - a.pout, 4, (long long)a.ld * a.h, kBsSweepStore))
+        *reinterpret_cast<V *>(out + cu.st_off) = Store<T>::from_f4(top);
+    if (PREV && outp && (unsigned)(cu.st_rel + 1) < (unsigned)rows &&
+        PFS_SPAN(outp + cu.st_off + a.ld - a.pprev, 4, (long long)a.ld * a.h, kBsSweepStorePrev))
         *reinterpret_cast<V *>(outp + cu.st_off + a.ld) = Store<T>::from_f4(N[L - 1]);
     if constexpr (RES) {
         TR[K % 3] = top;                                  // level L, row y-L

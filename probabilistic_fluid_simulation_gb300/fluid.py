@@ -28,7 +28,9 @@ from typing import Optional, Tuple
 import numpy as np
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "libpfs_gb300.so")
+# PFS_LIBRARY selects another build of the library, e.g. the bounds-checking
+# libpfs_gb300_bounds.so (build.build(bounds=True)).
+LIB_PATH = os.environ.get("PFS_LIBRARY") or os.path.join(_PKG, "libpfs_gb300.so")
 
 PFS_HOST, PFS_DEVICE = 0, 1
 PREC_F32, PREC_BF16, PREC_F16, PREC_F64, PREC_F32R = 0, 1, 2, 3, 4
@@ -76,6 +78,7 @@ SIGNATURES = [
     ("pfs_last_error", C.c_char_p, []),
     ("pfs_version", C.c_int, []),
     ("pfs_kernel_launches", C.c_longlong, []),
+    ("pfs_bounds_status", C.c_int, [C.POINTER(C.c_longlong)]),
     ("pfs_set_jacobi_iters", C.c_int, [C.c_int]),
     ("pfs_get_jacobi_iters", C.c_int, []),
     ("pfs_set_stream", C.c_int, [C.c_void_p]),
@@ -171,6 +174,15 @@ def get_jacobi_iters() -> int:
 def kernel_launches() -> int:
     """Kernels the library has launched since it was loaded."""
     return lib().pfs_kernel_launches()
+
+
+def bounds_status() -> dict:
+    """Read and clear the device-side bounds record of the bounds-checking build
+    (pfs_bounds_status in include/pfs.h); raises PFSError (unsupported) on the
+    normal build."""
+    out = (C.c_longlong * 5)()
+    _check(lib().pfs_bounds_status(out))
+    return {"count": out[0], "site": out[1], "line": out[2], "index": out[3], "extent": out[4]}
 
 
 def set_stream(stream_handle: int):
