@@ -162,7 +162,7 @@ __device__ __forceinline__ void prefetch_row(Cursor<T> &cu, typename Store<T>::V
 // the exact squared residual of level L at row y-L-1 (the row stored at the
 // previous step) into acc, with the per-cell arithmetic of the residual
 // kernels (residual_sq), for the stored lanes only.
-template <typename T, int L, bool PREV, bool RES, int K, int T0>
+template <typename T, int L, bool PREV, bool RES, int K, int T0, bool GUARD>
 __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB],
                                             float4 (&TR)[3], FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
                                             typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
@@ -174,7 +174,9 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
     float4(&P)[L] = R[K % 3];
     float4(&Cur)[L] = R[(K + 1) % 3];
     float4(&N)[L] = R[(K + 2) % 3];
-    if (t + D - 1 < nsteps) prefetch_row(cu, pr, br, (K + D - 1) % D, a);
+    // unguarded blocks copy rows past the task's last one as well: they lie in
+    // the plane (rows wrap) and land in slots whose rows are consumed
+    if (!GUARD || t + D - 1 < nsteps) prefetch_row(cu, pr, br, (K + D - 1) % D, a);
     cp_async_commit();
     cp_async_wait<D - 1>();  // row t has landed
     N[0] = Store<T>::to_f4(pr[(K % D) * 32]);  // zeros when a.pin is null (ring zero-filled)
@@ -209,23 +211,25 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
     cu.st_rel += 1;
 }
 
-template <typename T, int L, bool PREV, bool RES, int K, int T0>
+template <typename T, int L, bool PREV, bool RES, int K, int T0, bool GUARD = true>
 __device__ __forceinline__ void stream_steps(int t, float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB],
                                              float4 (&TR)[3], FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
                                              typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
                                              int nsteps, int rows, T *out, T *outp)
 {
     if constexpr (K < Ring<T, L, RES>::U) {
-        if (t + K < nsteps) {
-            stream_step<T, L, PREV, RES, K, T0>(t + K, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
-            stream_steps<T, L, PREV, RES, K + 1, T0>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+        if (!GUARD || t + K < nsteps) {
+            stream_step<T, L, PREV, RES, K, T0, GUARD>(t + K, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out,
+                                                       outp);
+            stream_steps<T, L, PREV, RES, K + 1, T0, GUARD>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out,
+                                                            outp);
         }
     }
 }
 
 // The ramp: the unrolled iterations I = 0, 1, ... whose first step I * U is
 // below 2L, with their step numbers known at compile time.
-template <typename T, int L, bool PREV, bool RES, int I>
+template <typename T, int L, bool PREV, bool RES, int I, bool GUARD>
 __device__ __forceinline__ void stream_ramp(float4 (&R)[3][L], float4 (&bq)[Ring<T, L, RES>::NB], float4 (&TR)[3],
                                             FFAcc2 (&acc)[2], typename Store<T>::Vec *pr,
                                             typename Store<T>::Vec *br, Cursor<T> &cu, const StreamArgs<T> &a,
@@ -233,8 +237,9 @@ __device__ __forceinline__ void stream_ramp(float4 (&R)[3][L], float4 (&bq)[Ring
 {
     constexpr int U = Ring<T, L, RES>::U;
     if constexpr (I * U < 2 * L) {
-        stream_steps<T, L, PREV, RES, 0, I * U>(I * U, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
-        stream_ramp<T, L, PREV, RES, I + 1>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+        stream_steps<T, L, PREV, RES, 0, I * U, GUARD>(I * U, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out,
+                                                       outp);
+        stream_ramp<T, L, PREV, RES, I + 1, GUARD>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
     }
 }
 template <int L, int U>
@@ -304,9 +309,16 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     TR[0] = TR[1] = TR[2] = z;
 
     constexpr int U = Ring<T, L, RES>::U;
-    stream_ramp<T, L, PREV, RES, 0>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
-    for (int t = ramp_steps<L, U>(); t < nsteps; t += U)
-        stream_steps<T, L, PREV, RES, 0, -1>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    if (nsteps >= ramp_steps<L, U>())
+        stream_ramp<T, L, PREV, RES, 0, false>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    else
+        stream_ramp<T, L, PREV, RES, 0, true>(R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    // whole blocks of U steps without per-step guards (one basic block, which
+    // the compiler can schedule across steps), then the guarded remainder
+    int t = ramp_steps<L, U>();
+    for (; t + U <= nsteps; t += U)
+        stream_steps<T, L, PREV, RES, 0, -1, false>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
+    if (t < nsteps) stream_steps<T, L, PREV, RES, 0, -1, true>(t, R, bq, TR, acc, pr, br, cu, a, nsteps, rows, out, outp);
     cp_async_wait<0>();
 }
 
