@@ -156,7 +156,7 @@ struct Field {
         red.ticket = ticket;
         red.nblocks = pfs::reduce_grid();
         // capacity for the fused check launches at chunks of 16 rows or more
-        const int ns = std::max(red.nblocks, pfs::sweep_stream_blocks(w, h, 16));
+        const int ns = std::max(red.nblocks, pfs::sweep_stream_blocks(w, h, pfs::kMinChunkRows));
         CK(cudaMalloc(&psweep, 2 * (size_t)ns * sizeof(double)));
         red_sweep = red;
         red_sweep.partials = psweep;

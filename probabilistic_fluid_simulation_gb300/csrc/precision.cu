@@ -969,7 +969,7 @@ int lp_create(LpState **out, int form, int w, int h, int iw, int ih, int ic)
     if (form == PFS_PREC_F32R) {
         // the correction solve's checks: partials for the fused check launches at chunks of 16 rows or
         // more and for the scale kernel's norm | result pair | two tickets
-        const int ns = std::max(reduce_grid(), sweep_stream_blocks(w, h, 16));
+        const int ns = std::max(reduce_grid(), sweep_stream_blocks(w, h, kMinChunkRows));
         const size_t ibytes = (2 * (size_t)ns + 2) * sizeof(double) + 16;
         e = cudaMalloc(&s->in_mem, ibytes);
         if (e == cudaSuccess) e = cudaMemset(s->in_mem, 0, ibytes);

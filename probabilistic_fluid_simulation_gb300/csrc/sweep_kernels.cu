@@ -46,26 +46,25 @@ __global__ void k_sweep_single(const float *__restrict__ pin, const float *__res
 
 int stream_strip_width(int halo) { return 128 - 2 * halo; }
 
-// Each warp task recomputes 2L halo rows besides its chunk, so taller chunks
-// waste less; but every scheduler needs warps to hide the sweep's dependent
-// FP32 latency, and a grid with fewer tasks than one wave of resident warps
-// leaves SMs idle. The default is the tallest chunk of 16, 32, 64 or 128 rows
-// that still gives 90% of a wave (four warps per block, the blocks per SM the
-// kernel's launch bounds allow, every SM); smaller grids take 16. Measured on
-// GB300, 8 sweeps per launch: 2048x2048 best at 32 rows; 4096x4096 59.7 us at
-// 32, 51.5 us at 64.
+// Chunk height by grid. A warp task recomputes L(L-1) level rows besides its
+// chunk (after the ramp skip), so taller chunks waste less; but a grid with
+// more tasks than one wave of resident warps runs a second, mostly empty
+// wave, and one with fewer leaves schedulers without their warps. The default
+// is the smallest chunk that fits the grid in one wave (four warps per
+// block, the blocks per SM the kernel is held to, every SM), at least
+// kMinChunkRows. Measured on GB300, 8 sweeps per launch (us per launch, the
+// default marked *): 4096^2 128* 33.9, 64 37.3; 2048^2 32* 10.6, 16 13.5;
+// 1024^2 9* 5.77, 10 6.0, 16 7.2; 512^2 4* 5.18, 16 5.91; 1536^2 22 8.7,
+// 16 10.8.
 int default_chunk(int w, int h, int levels)
 {
     const int halo = levels <= 4 ? 4 : 8;
-    const int nsx = (w + stream_strip_width(halo) - 1) / stream_strip_width(halo);
+    const long long nsx = (w + stream_strip_width(halo) - 1) / stream_strip_width(halo);
     const int sms = device_sms() > 0 ? device_sms() : 1;
     const long long wave = (long long)sms * 4 * (levels >= 7 ? min_blocks<8>() : min_blocks<4>());
-    int best = 16;
-    for (int c = 32; c <= 128; c *= 2) {
-        const long long tasks = (long long)nsx * ((h + c - 1) / c);
-        if (10 * tasks >= 9 * wave) best = c;
-    }
-    return best;
+    const long long per = std::max(1LL, wave / std::max(1LL, nsx));  // row chunks one wave holds
+    const long long c = (h + per - 1) / per;
+    return (int)std::max<long long>(kMinChunkRows, std::min<long long>(c, std::max(h, 1)));
 }
 
 cudaError_t launch_sweep_single(const float *pin, const float *b, float *pout, int ld, int w, int h,

@@ -118,12 +118,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Offsets count vectors of four cells (16 B in float32), which keeps them in
+// 32 bits for planes below 2^33 cells (launch_stream_t checks): each address
+// is then one wide multiply-add from the plane's base, and the periodic wrap
+// of the copied rows one compare and subtract.
 template <typename T>
 struct Cursor {
-    const T *gp, *gb;      // next row to prefetch (p and b planes, lane column)
-    int ld_row;            // its row index (wrapped)
-    long long st_off;      // offset of the level-L row of this step, in elements from the lane column
-    int st_rel;            // that row minus y0 (stored when 0 <= st_rel < rows)
+    int off;     // vector offset of the next row to copy (lane column), the same in the p and b planes
+    int st_vo;   // vector offset of this step's level-L row from the lane column
+    int st_rel;  // that row minus y0 (stored when 0 <= st_rel < rows)
 };
 
 // Issue the cp.async of the next row into ring slot `slot` of p and b.
@@ -131,19 +134,16 @@ template <typename T>
 __device__ __forceinline__ void prefetch_row(Cursor<T> &cu, typename Store<T>::Vec *pr, typename Store<T>::Vec *br,
                                              int slot, const StreamArgs<T> &a)
 {
+    using V = typename Store<T>::Vec;
     constexpr int VB = Store<T>::vec_bytes;
     const long long n = (long long)a.ld * a.h;  // plane extent (checked build)
     (void)n;
-    if (a.pin && PFS_SPAN(cu.gp - a.pin, 4, n, kBsSweepLoadP)) cp_async<VB>(pr + slot * 32, cu.gp);
-    if (PFS_SPAN(cu.gb - a.b, 4, n, kBsSweepLoadB)) cp_async<VB>(br + slot * 32, cu.gb);
-    if (++cu.ld_row == a.h) {
-        cu.ld_row = 0;
-        cu.gp -= (size_t)(a.h - 1) * a.ld;
-        cu.gb -= (size_t)(a.h - 1) * a.ld;
-    } else {
-        cu.gp += a.ld;
-        cu.gb += a.ld;
-    }
+    const int ldv = a.ld >> 2, hv = a.h * ldv;  // row and plane, in vectors
+    if (a.pin && PFS_SPAN(4LL * cu.off, 4, n, kBsSweepLoadP))
+        cp_async<VB>(pr + slot * 32, reinterpret_cast<const V *>(a.pin) + cu.off);
+    if (PFS_SPAN(4LL * cu.off, 4, n, kBsSweepLoadB)) cp_async<VB>(br + slot * 32, reinterpret_cast<const V *>(a.b) + cu.off);
+    cu.off += ldv;
+    if (cu.off >= hv) cu.off -= hv;
 }
 
 // One row step t of the pipeline (load row y = ybeg + t); K = t mod U is a
@@ -190,12 +190,13 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
         if (s + 1 < L) N[s + 1] = o;
         else top = o;
     }
+    const int ldv = a.ld >> 2;
     if (out && (unsigned)cu.st_rel < (unsigned)rows &&
-        PFS_SPAN(out + cu.st_off - a.pout, 4, (long long)a.ld * a.h, kBsSweepStore))
-        *reinterpret_cast<V *>(out + cu.st_off) = Store<T>::from_f4(top);
+        PFS_SPAN(out + 4LL * cu.st_vo - a.pout, 4, (long long)a.ld * a.h, kBsSweepStore))
+        reinterpret_cast<V *>(out)[cu.st_vo] = Store<T>::from_f4(top);
     if (PREV && outp && (unsigned)(cu.st_rel + 1) < (unsigned)rows &&
-        PFS_SPAN(outp + cu.st_off + a.ld - a.pprev, 4, (long long)a.ld * a.h, kBsSweepStorePrev))
-        *reinterpret_cast<V *>(outp + cu.st_off + a.ld) = Store<T>::from_f4(N[L - 1]);
+        PFS_SPAN(outp + 4LL * (cu.st_vo + ldv) - a.pprev, 4, (long long)a.ld * a.h, kBsSweepStorePrev))
+        reinterpret_cast<V *>(outp)[cu.st_vo + ldv] = Store<T>::from_f4(N[L - 1]);
     if constexpr (RES) {
         TR[K % 3] = top;                                  // level L, row y-L
         const float4 &c = TR[(K + 2) % 3];                // row y-L-1
@@ -207,7 +208,7 @@ __device__ __forceinline__ void stream_step(int t, float4 (&R)[3][L], float4 (&b
             residual_sq4(acc, bb, lft, c, rgt, up, top);
         }
     }
-    cu.st_off += a.ld;
+    cu.st_vo += ldv;
     cu.st_rel += 1;
 }
 
@@ -285,12 +286,11 @@ __device__ __forceinline__ void stream_task(const StreamArgs<T> &a, int wid, int
     }
 
     Cursor<T> cu;
-    cu.ld_row = ybeg % a.h;
-    if (cu.ld_row < 0) cu.ld_row += a.h;
-    cu.gp = a.pin + (size_t)cu.ld_row * a.ld + cx;
-    cu.gb = a.b + (size_t)cu.ld_row * a.ld + cx;
+    int ld_row = ybeg % a.h;
+    if (ld_row < 0) ld_row += a.h;
+    cu.off = ld_row * (a.ld >> 2) + (cx >> 2);  // cx and ld are multiples of 4
     cu.st_rel = -E - L;  // level L at step 0 is row ybeg - L = y0 - E - L
-    cu.st_off = (long long)(y0 - E - L) * a.ld;
+    cu.st_vo = (y0 - E - L) * (a.ld >> 2);
     T *out = st_lane ? a.pout + cx : nullptr;
     T *outp = (PREV && st_lane) ? a.pprev + cx : nullptr;
 #pragma unroll
