@@ -221,7 +221,10 @@ struct StepOut {
     bool stalled = false;
 };
 
-bool fused_ok(const Field &f) { return f.w % 4 == 0; }
+// The fused sweep needs rows of whole float4 vectors and addresses them by
+// 32-bit vector offsets (planes below 2^33 cells); other grids take the
+// single-sweep kernel.
+bool fused_ok(const Field &f) { return f.w % 4 == 0 && (long long)f.h * (f.ld / 4) < (1LL << 31); }
 
 // Sum r^2 of pressure plane `pp` and read back (r^2, b^2) (b^2 from the last divergence).
 int residual_host(Field &f, const float *pp, cudaStream_t st, double &rr, double &bb)
@@ -1386,6 +1389,8 @@ int pfs_pressure_sweeps(const float *p_in, const float *b, float *p_out, float *
         if (vx % 4 || ld % 4 || ((uintptr_t)p_in | (uintptr_t)b | (uintptr_t)p_out | (uintptr_t)p_prev) % 16)
             return fail(PFS_ERR_UNSUPPORTED, "fused sweeps need vx %% 4 == 0, ld %% 4 == 0, 16-byte planes");
         if (levels > 8) return fail(PFS_ERR_UNSUPPORTED, "fused sweeps: at most 8 levels per call");
+        if ((long long)vy * (ld / 4) >= (1LL << 31))
+            return fail(PFS_ERR_UNSUPPORTED, "fused sweeps: planes must hold fewer than 2^33 cells");
         const int halo = levels <= 4 ? 4 : 8;
         CK(pfs::launch_sweep_stream(p_in, b, p_out, p_prev, ld, vx, vy, levels, halo,
                                     chunk_rows > 0 ? chunk_rows : pfs::default_chunk(vx, vy, levels), nullptr, st));
