@@ -699,13 +699,14 @@ int pfs_ensemble_create(pfs_ensemble **out, int n, const int *w, const int *h, i
     if (p.max_iters <= 0 || p.max_iters % L || (p.check_every > 0 && p.check_every % L))
         return pfs::record_error(PFS_ERR_UNSUPPORTED, "ensemble sweep cap and check interval must be multiples of "
                                                       "the fuse depth");
-    for (int k = 0; k < n; ++k)
+    for (int k = 0; k < n; ++k) {
         if (w[k] <= 0 || h[k] <= 0 || w[k] % 4)
             return pfs::record_error(PFS_ERR_INVALID_ARGUMENT, "member widths must be positive multiples of 4");
         // the sweep task addresses rows by 32-bit offsets in vectors of four cells (its row pitch is
         // the width rounded up to 32)
         if ((long long)h[k] * ((w[k] + 31) / 32 * 32 / 4) >= (1LL << 31))
             return pfs::record_error(PFS_ERR_UNSUPPORTED, "member planes must hold fewer than 2^33 cells");
+    }
     Ensemble *E = new (std::nothrow) Ensemble();
     if (!E) return pfs::record_error(PFS_ERR_CUDA, "out of host memory");
     E->n = n;
