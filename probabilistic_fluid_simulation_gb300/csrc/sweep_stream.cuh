@@ -70,10 +70,11 @@ struct StreamArgs {
     int stall_window;    // > 0: stop when the residual stops falling (SolveState)
 };
 
-// Warps per block of the standalone sweep kernel. Registers bound its
-// occupancy: each of an SM's four schedulers holds 16384 registers, so at
-// the 8-level kernel's 176 registers per thread a scheduler takes two warps
-// whatever the block size (blocks of two warps measured the same as four).
+// Warps per block of the standalone sweep kernel. Each of an SM's four
+// schedulers holds 16384 registers, so the warps a scheduler can take follow
+// from the registers per thread whatever the block size (at 176 registers,
+// blocks of two warps measured the same as four); the 7- and 8-level kernels
+// are held at two blocks per SM, two warps per scheduler (launch_stream_t).
 constexpr int kStreamWarps = 4;
 
 constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
