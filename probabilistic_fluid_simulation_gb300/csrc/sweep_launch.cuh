@@ -61,12 +61,14 @@ template <typename T, int G, int L, bool PREV, bool RES = false>
 cudaError_t launch_stream_t(const StreamArgs<T> &a, cudaStream_t st)
 {
     // The deepest pipelines (L >= 7) are sized for two blocks per SM
-    // (min_blocks; default_chunk fills that wave). Their register use can fall
-    // low enough for a third block, and such a grid then lands unevenly on the
-    // SMs (4096^2 at 128-row chunks: 34 -> 44 us per launch). A shared-memory
-    // request above a third of the SM's 228 KB keeps them at two.
+    // (min_blocks; default_chunk fills that wave), and the check launches run
+    // on the same chunks. Their register use can fall low enough for a third
+    // block, and such a grid then lands unevenly on the SMs (4096^2 at 128-row
+    // chunks: 34 -> 44 us per launch; the 4-level check at 148 registers cost
+    // 1.5% of a capped 2048^2 step). A shared-memory request above a third of
+    // the SM's 228 KB keeps them at two.
     constexpr int ring_bytes = kStreamWarps * Ring<T, L, RES>::vecs_per_warp * Store<T>::vec_bytes;
-    constexpr int smem = (L >= 7 && ring_bytes < 76 * 1024) ? 76 * 1024 : ring_bytes;
+    constexpr int smem = ((L >= 7 || RES) && ring_bytes < 76 * 1024) ? 76 * 1024 : ring_bytes;
     static std::atomic<unsigned long long> attr_done{0};  // per instantiation and device
     const cudaError_t e = smem_limit_once(k_sweep_stream<T, G, L, PREV, RES>, smem, attr_done);
     if (e != cudaSuccess) return e;
