@@ -236,7 +236,9 @@ def test_full_size_2048_one_step_to_residual(cuda_device, pfs_lib, oracle_mod):
 # ---------------------------------------------------------------------------------------------
 # Kernel-level: the fused (temporally blocked) sweep equals repeated single sweeps
 
-@pytest.mark.parametrize("w,h", [(2048, 2048), (1024, 200), (260, 132), (128, 128), (64, 64), (12, 8), (4, 3)])
+# default chunk heights from 4 rows (1024x200, 128x128) to 18 (1536^2), 32 (2048^2) and 128 (4096^2)
+@pytest.mark.parametrize("w,h", [(4096, 4096), (2048, 2048), (1536, 1536), (1024, 200), (260, 132), (128, 128),
+                                 (64, 64), (12, 8), (4, 3)])
 @pytest.mark.parametrize("levels", [1, 2, 5, 8])
 def test_fused_sweeps_equal_single_sweeps(cuda_device, pfs_lib, w, h, levels):
     import torch
@@ -258,7 +260,7 @@ def test_fused_sweeps_equal_single_sweeps(cuda_device, pfs_lib, w, h, levels):
         assert torch.equal(prev[:, :w], p[:, :w])
 
 
-@pytest.mark.parametrize("chunk", [8, 17, 32, 64, 200])
+@pytest.mark.parametrize("chunk", [4, 8, 9, 17, 18, 32, 64, 200])
 def test_fused_sweep_chunking(cuda_device, pfs_lib, chunk):
     import torch
     g = torch.Generator(device="cpu").manual_seed(chunk)
