@@ -145,7 +145,9 @@ int pfs_advect_color_step_host(pfs_vp_field *image, pfs_vp_field *itmp, pfs_vp_f
 enum { PFS_HOST = 0, PFS_DEVICE = 1 };
 
 /* Storage / arithmetic form of a session:
- *   PFS_PREC_F32   the reference's float32 arithmetic, bit-exact (default);
+ *   PFS_PREC_F32   the reference's float32 arithmetic, bit-exact (default; the fused sweep's
+ *                  final multiply-add on b/4 rounds as the reference does for every value in
+ *                  float32's normal range, above about 5e-38 in magnitude);
  *   PFS_PREC_BF16  velocity, image and the pressure correction stored bf16,
  *                  computed in FP32; the pressure held as a pair of floats
  *                  (about 48 significant bits), its residual and the
