@@ -132,6 +132,17 @@ __device__ bool grid_sync(const EnsArgs &a)
 template <typename T>
 __device__ __forceinline__ T vload(const T &x) { return *(const volatile T *)&x; }
 
+// A member's (cur, done) in one 8-byte load: every sweep and residual task
+// reads both before it starts, and they change between phases.
+static_assert(offsetof(MemberState, done) == offsetof(MemberState, cur) + sizeof(int) &&
+                  offsetof(MemberState, cur) % 8 == 0 && alignof(MemberState) >= 8,
+              "cur and done must share one aligned 8-byte word");
+__device__ __forceinline__ int2 state_cur_done(const MemberState &ms)
+{
+    const unsigned long long v = *reinterpret_cast<const volatile unsigned long long *>(&ms.cur);
+    return make_int2((int)(unsigned)(v & 0xffffffffull), (int)(unsigned)(v >> 32));  // little-endian: cur first
+}
+
 __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll
@@ -287,8 +298,9 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
     for (int s = 0; s < a.cap;) {
         for (int t = gw; t < a.nsw_tasks; t += nw) {
             const int mi = a.sw_member[t];
-            if (vload(a.state[mi].done)) continue;
-            const int cur = vload(a.state[mi].cur);
+            const int2 cd = state_cur_done(a.state[mi]);  // one L2 round trip for both words
+            if (cd.y) continue;
+            const int cur = cd.x;
             const Member &m = a.mem[mi];
             StreamArgs<float> sa;
             sa.pin = (REF && vload(a.state[mi].zero_phase) == phase) ? nullptr : m.p[(cur + phase) & 1];
@@ -310,8 +322,9 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         if (s % a.check_every != 0 && s != a.cap) continue;
         for (int t = gw; t < a.nrs_tasks; t += nw) {
             const int mi = a.rs_member[t];
-            if (vload(a.state[mi].done)) continue;
-            const int cur = vload(a.state[mi].cur);
+            const int2 cd = state_cur_done(a.state[mi]);  // one L2 round trip for both words
+            if (cd.y) continue;
+            const int cur = cd.x;
             const Member &m = a.mem[mi];
             const int q = t - m.rs_task0, sx = q % m.rsx, sy = q / m.rsx;
             const int y0 = sy * 8, y1 = min(m.h, y0 + 8);
