@@ -295,15 +295,29 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
 
     // pressure: phases of L fused sweeps; residual checks every check_every sweeps and at the cap
     int phase = 0, check = 0;
+    // The member state a sweep task reads (plane index, done flag, and for the
+    // refined form the phase whose correction starts at zero) changes only in
+    // the check below, so the warp keeps its first task's reading from one
+    // check to the next instead of an L2 round trip per phase.
+    int c_mi = 0, c_cur = 0, c_done = 0, c_zero = -1;
+    bool cached = false;
     for (int s = 0; s < a.cap;) {
         for (int t = gw; t < a.nsw_tasks; t += nw) {
-            const int mi = a.sw_member[t];
-            const int2 cd = state_cur_done(a.state[mi]);  // one L2 round trip for both words
-            if (cd.y) continue;
-            const int cur = cd.x;
+            int mi, cur, dn, zp;
+            if (t == gw && cached) {
+                mi = c_mi, cur = c_cur, dn = c_done, zp = c_zero;
+            } else {
+                mi = a.sw_member[t];
+                const int2 cd = state_cur_done(a.state[mi]);  // one L2 round trip for both words
+                cur = cd.x;
+                dn = cd.y;
+                zp = REF ? vload(a.state[mi].zero_phase) : -1;
+                if (t == gw) c_mi = mi, c_cur = cur, c_done = dn, c_zero = zp, cached = true;
+            }
+            if (dn) continue;
             const Member &m = a.mem[mi];
             StreamArgs<float> sa;
-            sa.pin = (REF && vload(a.state[mi].zero_phase) == phase) ? nullptr : m.p[(cur + phase) & 1];
+            sa.pin = (REF && zp == phase) ? nullptr : m.p[(cur + phase) & 1];
             sa.pout = m.p[(cur + phase + 1) & 1];
             sa.b = m.b;
             sa.pprev = nullptr;
@@ -320,6 +334,7 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         s += L;
         if (!grid_sync(a)) return;
         if (s % a.check_every != 0 && s != a.cap) continue;
+        cached = false;  // the check may change done, cur and zero_phase
         for (int t = gw; t < a.nrs_tasks; t += nw) {
             const int mi = a.rs_member[t];
             const int2 cd = state_cur_done(a.state[mi]);  // one L2 round trip for both words
