@@ -619,12 +619,14 @@ def headline_forms(a, fluid, synthetic, stream):
                rounding floor), reported with the time to reach it;
     plain      the plain method that reaches 1e-5 (PFS_PREC_F32R): the same
                float32 Jacobi sweeps (the plain form's kernels), with the
-               pressure accumulated in FP64 and refined only when the float32
-               correction reaches its floor; the reference's previous-pressure
-               start. Every ratio is against this row;
+               pressure accumulated as a pair of floats (about 48 bits) and
+               refined when the float32 correction has run its interval or
+               meets the tolerance; the reference's previous-pressure start.
+               Every ratio is against this row;
     zero_start the same from zero pressure each step;
-    bf16, f16  the precision forms (16-bit storage, FP32 compute, FP64
-               residual and refinement), to 1e-5 or to their floor;
+    bf16, f16  the precision forms (16-bit storage, FP32 compute, float-pair
+               pressure, residual and refinement in error-free float32
+               arithmetic), to 1e-5 or to their floor;
     network    the learned warm start (the shipped network on the grid
                coarsened 8x, 8 damped passes), then the plain iteration;
     batched    the ensemble form on the headline state together with smaller
