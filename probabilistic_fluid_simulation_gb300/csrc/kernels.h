@@ -173,6 +173,11 @@ cudaError_t launch_sweep_stream(const float *pin, const float *b, float *pout, f
 // with sweeps_here). Needs red.nblocks >= sweep_stream_blocks(w, h, chunk);
 // red.result[1] must hold sum b^2.
 int sweep_stream_blocks(int w, int h, int chunk);
+// launch_sweep_stream_check without the level L-1 output (pprev null), in its own unit.
+cudaError_t launch_sweep_stream_check_noprev(const float *pin, const float *b, float *pout, int ld, int w, int h,
+                                             int levels, int chunk, const Reduce &red, SolveState *state,
+                                             int sweeps_here, double tol, const int *done, cudaStream_t st,
+                                             int stall_window);
 // Smallest row chunk default_chunk picks (partial sums of the fused check are sized for it).
 constexpr int kMinChunkRows = 4;
 cudaError_t launch_sweep_stream_check(const float *pin, const float *b, float *pout, float *pprev, int ld, int w,

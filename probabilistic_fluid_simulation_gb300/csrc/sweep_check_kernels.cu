@@ -26,15 +26,19 @@ cudaError_t launch_sweep_stream_check(const float *pin, const float *b, float *p
     a.sweeps_here = sweeps_here;
     a.tol = tol;
     a.stall_window = stall_window;
-    const bool prev = pprev != nullptr;
+    // without the level L-1 output (the refined forms' correction solves): the
+    // other unit, so that the two halves of the instantiations compile in parallel
+    if (!pprev)
+        return launch_sweep_stream_check_noprev(pin, b, pout, ld, w, h, levels, chunk, red, state, sweeps_here, tol,
+                                                done, st, stall_window);
     switch (levels) {
-    case 1: return prev ? launch_stream_t<float, 8, 1, true, true>(a, st) : launch_stream_t<float, 8, 1, false, true>(a, st);
-    case 2: return prev ? launch_stream_t<float, 8, 2, true, true>(a, st) : launch_stream_t<float, 8, 2, false, true>(a, st);
-    case 3: return prev ? launch_stream_t<float, 8, 3, true, true>(a, st) : launch_stream_t<float, 8, 3, false, true>(a, st);
-    case 4: return prev ? launch_stream_t<float, 8, 4, true, true>(a, st) : launch_stream_t<float, 8, 4, false, true>(a, st);
-    case 5: return prev ? launch_stream_t<float, 8, 5, true, true>(a, st) : launch_stream_t<float, 8, 5, false, true>(a, st);
-    case 6: return prev ? launch_stream_t<float, 8, 6, true, true>(a, st) : launch_stream_t<float, 8, 6, false, true>(a, st);
-    case 7: return prev ? launch_stream_t<float, 8, 7, true, true>(a, st) : launch_stream_t<float, 8, 7, false, true>(a, st);
+    case 1: return launch_stream_t<float, 8, 1, true, true>(a, st);
+    case 2: return launch_stream_t<float, 8, 2, true, true>(a, st);
+    case 3: return launch_stream_t<float, 8, 3, true, true>(a, st);
+    case 4: return launch_stream_t<float, 8, 4, true, true>(a, st);
+    case 5: return launch_stream_t<float, 8, 5, true, true>(a, st);
+    case 6: return launch_stream_t<float, 8, 6, true, true>(a, st);
+    case 7: return launch_stream_t<float, 8, 7, true, true>(a, st);
     default: return cudaErrorInvalidValue;
     }
 }
