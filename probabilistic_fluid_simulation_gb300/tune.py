@@ -2,12 +2,16 @@
 
     python -m probabilistic_fluid_simulation_gb300.tune --size 2048 --levels 8 --chunk 32
     python -m probabilistic_fluid_simulation_gb300.tune --size 2048 --scan
+    python -m probabilistic_fluid_simulation_gb300.tune --size 2048 --ensemble 1 --ens-sweeps 64
 
 Times back-to-back launches of `levels` fused sweeps on random planar
 fields with CUDA events on the launching stream and prints microseconds per
 launch and cell-sweeps per second. --scan times every (levels, chunk rows)
 candidate and prints the fastest; `best_config` is the same search as a
 function (used to pick a session's fuse depth and chunk height).
+--ensemble N times the step of the batched form (one persistent launch) on N
+grids of that size instead; `tune_ensemble` picks an ensemble's fuse depth
+and chunk height.
 """
 from __future__ import annotations
 
@@ -87,6 +91,28 @@ def tune_ensemble(ens, steps: int = 1, candidates=ENSEMBLE_CANDIDATES):
     return best, timings
 
 
+def time_ensemble(w: int, h: int, members: int, levels: int, chunk: int, sweeps: int, reps: int = 3) -> float:
+    """ms per step of an ensemble of `members` w x h vortex states (float32,
+    `sweeps` pressure sweeps per step, no residual checks), CUDA events around
+    `reps` steps after one untimed step."""
+    import torch
+    from probabilistic_fluid_simulation_gb300 import synthetic
+    kw = dict(dt=0.05, diffuse_iters=40, max_iters=sweeps, tol=0.0, check_every=0, fuse_depth=levels,
+              chunk_rows=chunk or 32)
+    with fluid.Ensemble([(w, h)] * members, 3, **kw) as ens:
+        for k in range(members):
+            vp, tmp, img, _ = synthetic.initial_state(w, h, 3, seed=k)
+            ens.upload(k, vp, tmp, img)
+        ens.step(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ens.step(reps)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, default=2048)
@@ -96,9 +122,16 @@ def main():
     ap.add_argument("--reps", type=int, default=100)
     ap.add_argument("--scan", action="store_true")
     ap.add_argument("--scan-levels", default=",".join(str(x) for x in LEVELS), help="fuse depths for --scan")
+    ap.add_argument("--ensemble", type=int, default=0,
+                    help="time the step of an ensemble of this many --size grids instead (the batched form)")
+    ap.add_argument("--ens-sweeps", type=int, default=2000, help="pressure sweeps per ensemble step")
     a = ap.parse_args()
     cells = a.size * (a.height or a.size)
-    if a.scan:
+    if a.ensemble:
+        ms = time_ensemble(a.size, a.height or a.size, a.ensemble, a.levels, a.chunk, a.ens_sweeps, a.reps)
+        print(json.dumps({"size": a.size, "members": a.ensemble, "levels": a.levels, "sweeps": a.ens_sweeps,
+                          "ms_per_step": ms, "cell_sweeps_per_s": cells * a.ensemble * a.ens_sweeps / (ms * 1e-3)}))
+    elif a.scan:
         rows = []
         for lv in (int(x) for x in a.scan_levels.split(",")):
             for ch in CHUNKS:
