@@ -61,31 +61,42 @@ __device__ __forceinline__ Corners backtrace(int i, int j, float kx, float ky, f
     return c;
 }
 
-// Velocity advection of cell (i, j), src/fluid.cpp:24-70.
+// Velocity advection of cell (i, j), src/fluid.cpp:24-70: the new velocity
+// (uo, vo) without storing it.
+template <int BC = 0>
+__device__ __forceinline__ void advect_value(const float *__restrict__ u, const float *__restrict__ v, int ld, int w,
+                                             int h, float dt, int i, int j, float &uo, float &vo)
+{
+    const size_t o = (size_t)j * ld + i;
+    const long long n = (long long)ld * h;  // plane extent (checked build)
+    (void)n;
+    if (BC == 2 && on_edge(i, j, w, h)) {
+        uo = 0.0f;
+        vo = 0.0f;
+        return;
+    }
+    const Corners c = backtrace<BC>(i, j, dt, dt, PFS_LD(u, o, n, kBsAdvect), PFS_LD(v, o, n, kBsAdvect), (float)w,
+                                    (float)h, w, h);
+    const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
+    uo = bilerp(c.sx, c.sy, PFS_LD(u, r0 + c.i0, n, kBsAdvect), PFS_LD(u, r0 + c.i1, n, kBsAdvect),
+                PFS_LD(u, r1 + c.i0, n, kBsAdvect), PFS_LD(u, r1 + c.i1, n, kBsAdvect));
+    vo = bilerp(c.sx, c.sy, PFS_LD(v, r0 + c.i0, n, kBsAdvect), PFS_LD(v, r0 + c.i1, n, kBsAdvect),
+                PFS_LD(v, r1 + c.i0, n, kBsAdvect), PFS_LD(v, r1 + c.i1, n, kBsAdvect));
+}
+
+// Velocity advection of cell (i, j), stored.
 template <int BC = 0>
 __device__ __forceinline__ void advect_cell(const float *__restrict__ u, const float *__restrict__ v,
                                             float *__restrict__ uo, float *__restrict__ vo, int ld, int w, int h,
                                             float dt, int i, int j)
 {
     const size_t o = (size_t)j * ld + i;
-    const long long n = (long long)ld * h;  // plane extent (checked build)
+    const long long n = (long long)ld * h;
     (void)n;
-    if (BC == 2 && on_edge(i, j, w, h)) {
-        PFS_ST(uo, o, n, 0.0f, kBsAdvect);
-        PFS_ST(vo, o, n, 0.0f, kBsAdvect);
-        return;
-    }
-    const Corners c = backtrace<BC>(i, j, dt, dt, PFS_LD(u, o, n, kBsAdvect), PFS_LD(v, o, n, kBsAdvect), (float)w,
-                                    (float)h, w, h);
-    const size_t r0 = (size_t)c.j0 * ld, r1 = (size_t)c.j1 * ld;
-    PFS_ST(uo, o, n,
-           bilerp(c.sx, c.sy, PFS_LD(u, r0 + c.i0, n, kBsAdvect), PFS_LD(u, r0 + c.i1, n, kBsAdvect),
-                  PFS_LD(u, r1 + c.i0, n, kBsAdvect), PFS_LD(u, r1 + c.i1, n, kBsAdvect)),
-           kBsAdvect);
-    PFS_ST(vo, o, n,
-           bilerp(c.sx, c.sy, PFS_LD(v, r0 + c.i0, n, kBsAdvect), PFS_LD(v, r0 + c.i1, n, kBsAdvect),
-                  PFS_LD(v, r1 + c.i0, n, kBsAdvect), PFS_LD(v, r1 + c.i1, n, kBsAdvect)),
-           kBsAdvect);
+    float a, b;
+    advect_value<BC>(u, v, ld, w, h, dt, i, j, a, b);
+    PFS_ST(uo, o, n, a, kBsAdvect);
+    PFS_ST(vo, o, n, b, kBsAdvect);
 }
 
 // Divergence of cell (i, j) into b, src/fluid.cpp:218-237; returns it.

@@ -91,6 +91,9 @@ struct EnsArgs {
 // a 2048-row member over 2,048 tasks instead of 256 (at 8 rows per task its
 // three row phases took about 2.8 ms per step, most warps idle at the barrier).
 constexpr int kRowsPerTask = 1;
+// Cells a lane computes at once in the gather-bound row phases (advection,
+// projection with image advection).
+constexpr int kCellsInFlight = 4;
 constexpr long long kBarrierSpinLimit = 1LL << 24;  // ~1-2 s with the back-off below
 
 // Grid-wide barrier with a bounded wait. Returns false (and every later call
@@ -224,8 +227,23 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
     for (int t = gw; t < a.nrow_tasks; t += nw) {
         const Member &m = a.mem[a.row_member[t]];
         const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
+        // kCellsInFlight cells per lane at a time, all computed before any is
+        // stored, so that their dependent gathers overlap (lanes past the
+        // row's end compute its last cell and store nothing)
         for (int j = r0; j < r1; ++j)
-            for (int i = lane; i < m.w; i += 32) advect_cell(m.u[0], m.v[0], m.u[1], m.v[1], m.ld, m.w, m.h, a.dt, i, j);
+            for (int i0 = lane; i0 < m.w; i0 += 32 * kCellsInFlight) {
+                float ou[kCellsInFlight], ov[kCellsInFlight];
+#pragma unroll
+                for (int q = 0; q < kCellsInFlight; ++q)
+                    advect_value(m.u[0], m.v[0], m.ld, m.w, m.h, a.dt, min(i0 + 32 * q, m.w - 1), j, ou[q], ov[q]);
+#pragma unroll
+                for (int q = 0; q < kCellsInFlight; ++q)
+                    if (i0 + 32 * q < m.w) {
+                        const size_t o = (size_t)j * m.ld + i0 + 32 * q;
+                        m.u[1][o] = ou[q];
+                        m.v[1][o] = ov[q];
+                    }
+            }
     }
     if (!grid_sync(a)) return;
 
@@ -477,11 +495,42 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
                     ref_project_image_cell(m.u[1], m.v[1], m.x, m.u[0], m.v[0], m.p[0], m.ld, m.w, m.h, a.dt,
                                            m.img[ic], m.img[io], plane, a.channels, i, j);
         } else {
+            // as project_image_cell, kCellsInFlight cells per lane at a time (see
+            // the advection phase)
             const float *pf = m.p[vload(a.state[mi].cur)];
             for (int j = r0; j < r1; ++j)
-                for (int i = lane; i < m.w; i += 32)
-                    project_image_cell(m.u[1], m.v[1], pf, m.u[0], m.v[0], m.ld, m.w, m.h, a.dt, m.img[ic],
-                                       m.img[io], plane, a.channels, i, j);
+                for (int i0 = lane; i0 < m.w; i0 += 32 * kCellsInFlight) {
+                    float un[kCellsInFlight], vn[kCellsInFlight];
+                    Corners kc[kCellsInFlight];
+#pragma unroll
+                    for (int q = 0; q < kCellsInFlight; ++q)
+                        project_cell<0>(m.u[1], m.v[1], pf, m.ld, m.w, m.h, a.dt, min(i0 + 32 * q, m.w - 1), j, un[q],
+                                        vn[q]);
+#pragma unroll
+                    for (int q = 0; q < kCellsInFlight; ++q) {
+                        if (i0 + 32 * q < m.w) {
+                            const size_t o = (size_t)j * m.ld + i0 + 32 * q;
+                            m.u[0][o] = un[q];
+                            m.v[0][o] = vn[q];
+                        }
+                        kc[q] = backtrace<0>(min(i0 + 32 * q, m.w - 1), j, a.dt, a.dt, un[q], vn[q], (float)m.w,
+                                             (float)m.h, m.w, m.h);
+                    }
+                    for (int ch = 0; ch < a.channels; ++ch) {
+                        const float *sp = m.img[ic] + ch * plane;
+                        float *dp = m.img[io] + ch * plane;
+                        float val[kCellsInFlight];
+#pragma unroll
+                        for (int q = 0; q < kCellsInFlight; ++q) {
+                            const size_t r0k = (size_t)kc[q].j0 * m.ld, r1k = (size_t)kc[q].j1 * m.ld;
+                            val[q] = bilerp(kc[q].sx, kc[q].sy, sp[r0k + kc[q].i0], sp[r0k + kc[q].i1],
+                                            sp[r1k + kc[q].i0], sp[r1k + kc[q].i1]);
+                        }
+#pragma unroll
+                        for (int q = 0; q < kCellsInFlight; ++q)
+                            if (i0 + 32 * q < m.w) dp[(size_t)j * m.ld + i0 + 32 * q] = val[q];
+                    }
+                }
         }
     }
 }
