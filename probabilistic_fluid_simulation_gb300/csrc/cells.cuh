@@ -99,10 +99,9 @@ __device__ __forceinline__ void advect_cell(const float *__restrict__ u, const f
     PFS_ST(vo, o, n, b, kBsAdvect);
 }
 
-// Divergence of cell (i, j) into b, src/fluid.cpp:218-237; returns it.
-__device__ __forceinline__ float divergence_cell(const float *__restrict__ u, const float *__restrict__ v,
-                                                 float *__restrict__ b, int ld, int w, int h, float gamma, int i,
-                                                 int j)
+// Divergence of cell (i, j), src/fluid.cpp:218-237, without storing it.
+__device__ __forceinline__ float divergence_value(const float *__restrict__ u, const float *__restrict__ v, int ld,
+                                                  int w, int h, float gamma, int i, int j)
 {
     const size_t r = (size_t)j * ld;
     const long long n = (long long)ld * h;
@@ -110,8 +109,16 @@ __device__ __forceinline__ float divergence_cell(const float *__restrict__ u, co
     const float du = fsub(PFS_LD(u, r + wp(i, w), n, kBsDivergence), PFS_LD(u, r + wm(i, w), n, kBsDivergence));
     const float dv = fsub(PFS_LD(v, (size_t)wp(j, h) * ld + i, n, kBsDivergence),
                           PFS_LD(v, (size_t)wm(j, h) * ld + i, n, kBsDivergence));
-    const float bv = fmul(gamma, fadd(du, dv));
-    PFS_ST(b, r + i, n, bv, kBsDivergence);
+    return fmul(gamma, fadd(du, dv));
+}
+
+// Divergence of cell (i, j) into b; returns it.
+__device__ __forceinline__ float divergence_cell(const float *__restrict__ u, const float *__restrict__ v,
+                                                 float *__restrict__ b, int ld, int w, int h, float gamma, int i,
+                                                 int j)
+{
+    const float bv = divergence_value(u, v, ld, w, h, gamma, i, j);
+    PFS_ST(b, (size_t)j * ld + i, (long long)ld * h, bv, kBsDivergence);
     return bv;
 }
 

@@ -252,9 +252,22 @@ __global__ void __launch_bounds__(128, 2) k_ensemble_step(EnsArgs a)
         const Member &m = a.mem[a.row_member[t]];
         const int r0 = (t - m.row_task0) * kRowsPerTask, r1 = min(m.h, r0 + kRowsPerTask);
         FFAcc acc;
+        float *bo = REF ? m.bx : m.b;
+        // kCellsInFlight cells per lane at a time (see the advection phase); b^2 is added in the
+        // order of the cells, as one cell at a time would
         for (int j = r0; j < r1; ++j)
-            for (int i = lane; i < m.w; i += 32)
-                acc_square(acc, divergence_cell(m.u[1], m.v[1], REF ? m.bx : m.b, m.ld, m.w, m.h, a.gamma, i, j));
+            for (int i0 = lane; i0 < m.w; i0 += 32 * kCellsInFlight) {
+                float bv[kCellsInFlight];
+#pragma unroll
+                for (int q = 0; q < kCellsInFlight; ++q)
+                    bv[q] = divergence_value(m.u[1], m.v[1], m.ld, m.w, m.h, a.gamma, min(i0 + 32 * q, m.w - 1), j);
+#pragma unroll
+                for (int q = 0; q < kCellsInFlight; ++q)
+                    if (i0 + 32 * q < m.w) {
+                        bo[(size_t)j * m.ld + i0 + 32 * q] = bv[q];
+                        acc_square(acc, bv[q]);
+                    }
+            }
         const double s = warp_sum(acc.value());
         if (lane == 0) a.row_part[t] = s;
     }
